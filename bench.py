@@ -1,0 +1,410 @@
+"""Benchmark of the wavefront path tracer on one GB300 (or N replicas).
+
+Workload (default): the courtyard scene -- tessellated 30x12x20 room, 48
+cylinders of 2,048 triangles and 50,000 clutter triangles (268,304
+triangles, seeded) -- rendered at 1920x1080, 1 spp, path rays with 8
+bounces and 2 shadow samples per hit.  A step is one frame
+(Renderer::render): primary rays, shadow rays, 8 bounces of path rays with
+Morton keys, radix sort, reorder and traversal, shading, accumulation.
+
+Forms:
+  chosen  8-wide BVH with 8-bit quantised boxes, 64-bit 6-D Morton keys,
+          sort + reorder of path and shadow rays
+  plain   binary BVH with FP32 boxes, no sorting
+The headline value is the chosen form's rays per second over the whole
+frame (reference metric Mrays/s = rays * 1e-3 / ms, Renderer.cpp:692-706,
+here with everything in the frame timed).  The per-bounce microbenchmark
+traces one incoherent bounce wavefront with each form.
+
+Usage:
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+COURTYARD = dict(
+    scene_kind=1, seed=1, width=1920, height=1080,
+    camera=dict(position=(15.0, 5.0, 19.4), rotation_deg=(-8.0, 12.0, 0.0), fov_deg=60.0, znear=0.1, zfar=512.0),
+    light=(15.0, 11.0, 10.0), background=(0.529, 0.808, 0.98),
+    renderer=dict(ray_type=2, num_primary_samples=1, num_shadow_samples=2, shadow_radius=1.0, recursion_depth=8,
+                  key_value=0.6, white_point=2.0, albedo=0.8),
+)
+CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1,
+              reorder_shadow_rays=1)
+PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
+             reorder_shadow_rays=0)
+WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
+                 "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path and shadow rays")
+METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def setup_dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    world, rank, local = setup_dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    api = wf.api
+    lib = wf._lib.load()
+    W = COURTYARD
+    w, h = W["width"], W["height"]
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx)
+    geom = api.Geometry(pos, nrm, idx, device=dev)
+    cam = api.make_camera(**W["camera"])
+    stream = torch.cuda.current_stream()
+
+    def make(form):
+        r = api.Renderer(**W["renderer"], **form)
+        r.set_scene(scene, geom, W["light"], W["background"])
+        return r
+
+    px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+
+    def timed_frames(r, steps, warmup):
+        for _ in range(warmup):
+            r.render(cam, w, h, px, fp)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.wfpt_kernel_launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        rays = 0
+        ev0.record(stream)
+        for _ in range(steps):
+            r.render(cam, w, h, px, fp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        launches = lib.wfpt_kernel_launch_count() - l0
+        st = r.stats()
+        rays = (st.num_primary_rays + st.num_shadow_rays + st.num_path_rays) * steps
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        rt = torch.tensor([float(rays)], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.barrier()
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dist.all_reduce(rt, op=dist.ReduceOp.SUM)
+        return float(t.item()), float(rt.item()), st, launches
+
+    chosen = make(CHOSEN)
+    plain = make(PLAIN)
+    with ClockSampler(local) as clocks:
+        ms_c, rays_c, st_c, launches = timed_frames(chosen, args.steps, args.warmup)
+    ms_p, rays_p, st_p, _ = timed_frames(plain, args.steps, max(1, args.warmup // 2))
+    value = rays_c / (ms_c * 1e-3) / 1e6
+    plain_value = rays_p / (ms_p * 1e-3) / 1e6
+
+    # End to end through the C ABI with host buffers: per step the frame is
+    # rendered and the tone-mapped image is read back into pinned memory.
+    host_img = torch.empty((w * h, 4), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        chosen.render(cam, w, h, px, fp)
+        host_img.copy_(fp, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        chosen.render(cam, w, h, px, fp)
+        host_img.copy_(fp, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    rays_per_frame = st_c.num_primary_rays + st_c.num_shadow_rays + st_c.num_path_rays
+    e2e_value = rays_per_frame * args.steps / (e2e_ms * 1e-3) / 1e6 * world
+
+    micro = bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream)
+    hbm, peak_kind = peaks()
+    out = None
+    if rank == 0:
+        cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
+        tr = micro["trace_chosen"]
+        roof = {"kernel": "k_trace_bvh8 (closest hit, bounce-1 path rays after sort+reorder)", "bound": "hbm",
+                "achieved": tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                "frac": tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9 / hbm, "traffic": None,
+                "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_ray": 48}
+        srt = micro["sort"]
+        sort_roof = {"kernel": "radix sort u64 keys (63 bits, 8 passes) + u32 values", "bound": "hbm",
+                     "achieved": srt["gbs"], "peak": hbm, "unit": "GB/s", "frac": srt["gbs"] / hbm,
+                     "pairs": srt["n"], "alg_bytes_per_pair": 192}
+        out = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_c / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
+            "config": {"workload": WORKLOAD_NAME, "resolution": [w, h], "triangles": int(scene.info.num_triangles),
+                       "rays_per_frame": int(rays_per_frame),
+                       "path_rays_per_bounce": list(st_c.path_rays_per_bounce),
+                       "parallelism": f"replicas x{world}",
+                       "l2": "frame working set (>1 GB of ray/hit/key buffers) exceeds the 129 MB L2"},
+            "plain": {"value": round(plain_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_p / args.steps, 4),
+                      "rays_per_frame": int(st_p.num_primary_rays + st_p.num_shadow_rays + st_p.num_path_rays)},
+            "chosen_over_plain": round(value / plain_value, 3),
+            "per_bounce": micro["per_bounce"],
+            "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
+                             "reorder_gbs": round(micro["reorder"]["gbs"], 1),
+                             "reorder_frac": round(micro["reorder"]["gbs"] / hbm, 3)},
+            "roofline": roof, "sort_roofline": sort_roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 36,
+                    "d2h_bytes_per_step": w * h * 16,
+                    "note": "camera passed by value through the C ABI; tone-mapped frame read back to pinned host"},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(out))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
+    """One incoherent bounce: primary hits -> cosine bounce rays (bounce 1),
+    then traced plain (BVH2, unsorted) and chosen (6-D keys, sort, reorder,
+    BVH8).  Also times the sort and reorder kernels alone."""
+    import torch
+    n = w * h
+    i2p_np, _ = api.pixel_table(w, h)
+    i2p = torch.from_numpy(i2p_np).to(dev)
+    s2w = api.camera_screen_to_world(cam.position, cam.rotation_deg, cam.fov_deg, w / h, cam.znear, cam.zfar)
+    prim = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    api.raygen_primary(s2w, i2p, prim, list(cam.position), 0, w, h, cam.zfar)
+    hits = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    api.trace(scene, wf.BVH8_Q8, prim, hits)
+    seeds = torch.empty(n, dtype=torch.int32, device=dev)
+    api.init_seeds(seeds, 1)
+    dec = torch.ones((n, 4), dtype=torch.float32, device=dev)
+    path = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    p_i2p = torch.empty(n, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    api.raygen_path(seeds, geom.table, prim, path, i2p, p_i2p, hits, dec, cnt)
+    m = int(cnt.item())
+    path = path[:m].contiguous()
+    res = torch.empty((m, 4), dtype=torch.int32, device=dev)
+    smin = scene.bounds_min
+    ssize = scene.bounds_max - scene.bounds_min
+    keys = torch.empty(m, dtype=torch.int64, device=dev)
+    ids = torch.empty(m, dtype=torch.int32, device=dev)
+    scratch = torch.empty(api.sort_scratch_bytes(m, 64), dtype=torch.uint8, device=dev)
+    s2i = torch.arange(m, dtype=torch.int32, device=dev)
+    out = torch.empty_like(path)
+    os2i = torch.empty(m, dtype=torch.int32, device=dev)
+    oi2s = torch.empty(m, dtype=torch.int32, device=dev)
+
+    def timeit(fn, reps=10):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ms_plain = timeit(lambda: api.trace(scene, wf.BVH2_FP32, path, res))
+    ms_bvh8_unsorted = timeit(lambda: api.trace(scene, wf.BVH8_Q8, path, res))
+
+    def sort_part():
+        api.morton(path, smin, ssize, wf.MORTON_6D64, keys, ids)
+        api.sort_pairs(keys, ids, 63, scratch=scratch)
+
+    def composite():
+        sort_part()
+        api.reorder(ids, path, out, s2i, os2i, oi2s)
+        api.trace(scene, wf.BVH8_Q8, out, res)
+
+    ms_comp = timeit(composite)
+    sort_part()
+    api.reorder(ids, path, out, s2i, os2i, oi2s)
+    ms_trace8 = timeit(lambda: api.trace(scene, wf.BVH8_Q8, out, res))
+    ms_trace2_sorted = timeit(lambda: api.trace(scene, wf.BVH2_FP32, out, res))
+    ms_sort = timeit(lambda: api.sort_pairs(keys, ids, 63, scratch=scratch))
+    ms_morton = timeit(lambda: api.morton(path, smin, ssize, wf.MORTON_6D64, keys, ids))
+    ms_reorder = timeit(lambda: api.reorder(ids, path, out, s2i, os2i, oi2s))
+    mr = lambda ms: round(m / (ms * 1e-3) / 1e6, 2)
+    return {
+        "per_bounce": {"bounce": 1, "rays": m,
+                       "plain_mrays_s": mr(ms_plain), "chosen_composite_mrays_s": mr(ms_comp),
+                       "chosen_trace_only_mrays_s": mr(ms_trace8), "bvh8_unsorted_mrays_s": mr(ms_bvh8_unsorted),
+                       "bvh2_sorted_mrays_s": mr(ms_trace2_sorted),
+                       "chosen_over_plain_composite": round(ms_plain / ms_comp, 3),
+                       "chosen_over_plain_trace_only": round(ms_plain / ms_trace8, 3),
+                       "morton_ms": round(ms_morton, 4), "sort_ms": round(ms_sort, 4),
+                       "reorder_ms": round(ms_reorder, 4)},
+        "trace_chosen": {"ms": ms_trace8, "alg_bytes": 48.0 * m},
+        "sort": {"n": m, "ms": ms_sort, "gbs": 192.0 * m / (ms_sort * 1e-3) / 1e9},
+        "reorder": {"n": m, "ms": ms_reorder, "gbs": 80.0 * m / (ms_reorder * 1e-3) / 1e9},
+    }
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_frame(args, api, scene, pos, nrm, idx, w, h, form):
+    import oracle
+    W = COURTYARD
+    nodes, tris = scene.export_bvh2()
+    hg = oracle.HostGeometry(api.gltf_vertices(pos, nrm), idx)
+    c = W["camera"]
+    s2w = api.camera_screen_to_world(c["position"], c["rotation_deg"], c["fov_deg"], w / h, c["znear"], c["zfar"])
+    R = W["renderer"]
+    cfg = oracle.FrameCfg(ray_type=2, spp=1, S=R["num_shadow_samples"], depth=R["recursion_depth"],
+                          radius=R["shadow_radius"], key=R["key_value"], white=R["white_point"], albedo=R["albedo"],
+                          sort_shadow=form["sort_shadow_rays"], reorder_shadow=form["reorder_shadow_rays"],
+                          sort_path=form["sort_path_rays"], reorder_path=form["reorder_path_rays"],
+                          morton_kind=form["morton_kind"], frame_index=1)
+    t0 = time.perf_counter()
+    _, _, st = oracle.render_frame(nodes, tris, hg, scene.bounds_min, scene.bounds_max, W["light"],
+                                   W["background"], s2w, c["position"], c["zfar"], w, h, cfg)
+    dt = time.perf_counter() - t0
+    return (st.primary + st.shadow + st.path), dt
+
+
+def cpu_baseline(args, wf, api, scene, pos, nrm, idx):
+    import oracle
+    w, h = 480, 270
+    rays, dt = cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
+    return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"one {w}x{h} frame of the courtyard workload (1/16 of the pixels), chosen-form settings, "
+                      f"CPU oracle with FP32 BVH2 traversal; {int(rays)} rays in {dt:.2f} s"}
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args):
+    world, rank, local = setup_dist()
+    if rank != 0:
+        return None
+    import oracle
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    api = wf.api
+    W = COURTYARD
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx, host_only=True)
+    w, h = 480, 270
+    for _ in range(args.warmup):
+        cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
+    total_rays, total_t = 0, 0.0
+    for _ in range(args.steps):
+        r, dt = cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
+        total_rays += r
+        total_t += dt
+    value = total_rays / total_t / 1e6
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_t / args.steps * 1e3, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded scene)", "config": {"workload": WORKLOAD_NAME},
+           "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": oracle.num_threads(),
+                            "kind": "port",
+                            "sample": f"each step one {w}x{h} frame of the courtyard workload (1/16 of the "
+                                      "pixels) on the CPU restatement of the reference shaders (the reference's "
+                                      "Vulkan/rayQuery path is unavailable on this box)"},
+           "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""Whole frames through the C ABI renderer against the oracle's CPU frame
+(Renderer::render restated), bit-exact: same pixel table, seeds, rays,
+traversal, compaction order, shading and tone map."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def N(t):
+    return t.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def small(wf, orc, dev):
+    pos, nrm, idx = wf.api.generate_scene(0, 1, 65536)
+    sc = wf.api.Scene(pos, idx)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    nodes, tris = sc.export_bvh2()
+    hg = orc.HostGeometry(wf.api.gltf_vertices(pos, nrm), idx)
+    return sc, geom, nodes, tris, hg
+
+
+CAM = dict(position=(0.5, 0.5, 2.2), rotation_deg=(0.0, 0.0, 0.0), fov_deg=45.0, znear=0.001, zfar=10.0)
+LIGHT = (0.5, 1.6, 0.5)
+BG = (0.53, 0.81, 0.98)
+
+
+def run_pair(wf, orc, dev, small, w, h, frames=1, **opts):
+    import torch
+    sc, geom, nodes, tris, hg = small
+    base = dict(ray_type=wf.PATH_RAYS, num_primary_samples=1, num_shadow_samples=2, shadow_radius=0.1,
+                recursion_depth=4, key_value=0.6, white_point=2.0, sort_shadow_rays=0, reorder_shadow_rays=0,
+                sort_path_rays=0, reorder_path_rays=0, morton_kind=0, bvh_kind=wf.BVH2_FP32, albedo=0.8)
+    base.update(opts)
+    r = wf.api.Renderer(**base)
+    r.set_scene(sc, geom, LIGHT, BG)
+    cam = wf.api.make_camera(**CAM)
+    px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    s2w = wf.api.camera_screen_to_world(CAM["position"], CAM["rotation_deg"], CAM["fov_deg"], w / h, CAM["znear"],
+                                        CAM["zfar"])
+    cfg = orc.FrameCfg(ray_type=base["ray_type"], spp=base["num_primary_samples"], S=base["num_shadow_samples"],
+                       depth=base["recursion_depth"], radius=base["shadow_radius"], key=0.6, white=2.0, albedo=0.8,
+                       sort_shadow=base["sort_shadow_rays"], reorder_shadow=base["reorder_shadow_rays"],
+                       sort_path=base["sort_path_rays"], reorder_path=base["reorder_path_rays"],
+                       morton_kind=base["morton_kind"], frame_index=1)
+    o_px = None
+    for f in range(1, frames + 1):
+        r.render(cam, w, h, px, fp)
+        st = r.stats()
+        cfg.frame_index = f
+        o_px, o_fp, o_st = orc.render_frame(nodes, tris, hg, sc.bounds_min, sc.bounds_max, LIGHT, BG, s2w,
+                                            CAM["position"], CAM["zfar"], w, h, cfg, pixels=o_px)
+    assert wf.api.device_status() == 0
+    return N(px), N(fp), st, o_px, o_fp, o_st
+
+
+def same_bits(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+
+
+@pytest.mark.parametrize("opts", [
+    dict(),
+    dict(sort_path_rays=1, sort_shadow_rays=1),
+    dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1),
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1),
+    dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1, morton_kind=1,
+         num_shadow_samples=3),
+])
+def test_path_frame_bit_exact(wf, orc, dev, small, opts):
+    px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 96, 64, **opts)
+    assert st.num_primary_rays == o_st.primary
+    assert st.num_path_rays == o_st.path
+    assert st.num_shadow_rays == o_st.shadow
+    assert list(st.path_rays_per_bounce) == list(o_st.path_per_bounce)
+    assert same_bits(fp, o_fp) and same_bits(px, o_px)
+
+
+def test_small_config_full_size(wf, orc, dev, small):
+    """256x256, 4 bounces, 32-bit keys with reordering (the small config)."""
+    px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 256, 256, sort_path_rays=1, reorder_path_rays=1,
+                                            sort_shadow_rays=1, bvh_kind=1)
+    assert st.num_path_rays == o_st.path and st.num_shadow_rays == o_st.shadow
+    assert same_bits(fp, o_fp)
+
+
+@pytest.mark.parametrize("ray_type", [0, 1])
+def test_primary_and_shadow_frames(wf, orc, dev, small, ray_type):
+    px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 80, 50, ray_type=ray_type)
+    assert same_bits(fp, o_fp) and same_bits(px, o_px)
+
+
+def test_accumulation_over_frames_and_spp(wf, orc, dev, small):
+    px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 40, 40, frames=3, num_primary_samples=2,
+                                            sort_path_rays=1, reorder_path_rays=1)
+    assert same_bits(fp, o_fp) and same_bits(px, o_px)

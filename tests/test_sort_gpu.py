@@ -1,0 +1,121 @@
+"""Radix sort through the C ABI: bit-exact against a stable sort
+(the oracle's, i.e. the order any stable LSD sort produces), across sizes
+around tile boundaries, 32- and 64-bit keys, odd pass counts, partial key
+widths, device-side counts and clustered Morton keys."""
+import numpy as np
+import pytest
+
+from conftest import random_rays
+
+pytestmark = pytest.mark.gpu
+
+
+def T(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def N(t):
+    return t.cpu().numpy()
+
+
+def stable_ref(keys, key_bits):
+    mask = (1 << key_bits) - 1 if key_bits < 64 else (1 << 64) - 1
+    k = keys.astype(np.uint64) & np.uint64(mask)
+    order = np.argsort(k, kind="stable")
+    return keys[order], order.astype(np.uint32)
+
+
+def run_sort(wf, dev, keys, key_bits, n_dev=None):
+    import torch
+    is64 = key_bits > 32
+    dk = T(keys.view(np.int64 if is64 else np.int32), dev)
+    dv = torch.arange(keys.shape[0], dtype=torch.int32, device=dev)
+    wf.api.sort_pairs(dk, dv, key_bits, n_dev=None if n_dev is None else torch.tensor([n_dev], dtype=torch.int32,
+                                                                                       device=dev))
+    got_k = N(dk).view(np.uint64 if is64 else np.uint32)
+    got_v = N(dv).view(np.uint32)
+    return got_k, got_v
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 4095, 4096, 4097, 65536, 123457, (1 << 20) + 3])
+def test_sort_u32_sizes(wf, dev, n):
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint32)
+    k, v = run_sort(wf, dev, keys, 32)
+    rk, rv = stable_ref(keys, 32)
+    assert np.array_equal(k, rk) and np.array_equal(v, rv)
+    assert wf.api.device_status() == 0
+
+
+def test_sort_matches_oracle_with_duplicates(wf, orc, dev):
+    rng = np.random.default_rng(1)
+    keys = rng.integers(0, 64, 100000, dtype=np.uint32)  # heavy duplicates: stability matters
+    k, v = run_sort(wf, dev, keys, 32)
+    ok, ov = orc.sort_pairs(keys, np.arange(100000, dtype=np.uint32), 32)
+    assert np.array_equal(k, ok) and np.array_equal(v, ov)
+
+
+@pytest.mark.parametrize("key_bits", [63, 64, 48, 40, 33])
+def test_sort_u64(wf, dev, key_bits):
+    rng = np.random.default_rng(key_bits)
+    n = 300001
+    keys = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
+    keys[::7] = keys[3]  # duplicates
+    k, v = run_sort(wf, dev, keys, key_bits)
+    rk, rv = stable_ref(keys, key_bits)
+    assert np.array_equal(v, rv)
+    assert np.array_equal(k, rk)
+
+
+@pytest.mark.parametrize("key_bits", [8, 12, 24])
+def test_sort_partial_key_bits(wf, dev, key_bits):
+    rng = np.random.default_rng(key_bits)
+    keys = rng.integers(0, 2**32, 50000, dtype=np.uint32)
+    k, v = run_sort(wf, dev, keys, key_bits)
+    _, rv = stable_ref(keys, key_bits)
+    assert np.array_equal(v, rv)
+
+
+def test_sort_device_count(wf, dev):
+    rng = np.random.default_rng(7)
+    n, c = 200000, 123456
+    for bits in (32, 40):
+        keys = rng.integers(0, 2**32 if bits == 32 else 2**40, n, dtype=np.uint64)
+        keys = keys.astype(np.uint32) if bits == 32 else keys
+        k, v = run_sort(wf, dev, keys, bits, n_dev=c)
+        rk, rv = stable_ref(keys[:c], bits)
+        assert np.array_equal(v[:c], rv) and np.array_equal(k[:c], rk)
+        # elements past the device count are left untouched
+        assert np.array_equal(k[c:], keys[c:]) and np.array_equal(v[c:], np.arange(c, n, dtype=np.uint32))
+
+
+@pytest.mark.parametrize("kind,bits", [(0, 32), (1, 48), (2, 63)])
+def test_sort_clustered_morton_keys(wf, orc, dev, kind, bits):
+    """Morton keys of clustered 6-D Gaussian ray origins/directions."""
+    import torch
+    rng = np.random.default_rng(kind + 10)
+    n = 1 << 18
+    centers = rng.uniform(0.2, 0.8, (16, 3))
+    o = centers[rng.integers(0, 16, n)] + rng.normal(0, 0.02, (n, 3))
+    d = rng.normal(0, 1, (n, 3)) * 0.1 + np.array([0.3, -1.0, 0.2])
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = o
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    keys = torch.empty(n, dtype=torch.int32 if kind == 0 else torch.int64, device=dev)
+    idx = torch.empty(n, dtype=torch.int32, device=dev)
+    wf.api.morton(T(rays, dev), [0, 0, 0], [1, 1, 1], kind, keys, idx)
+    wf.api.sort_pairs(keys, idx, bits)
+    rk, ri = orc.morton(rays, [0, 0, 0], [1, 1, 1], kind)
+    sk, si = orc.sort_pairs(rk, ri, bits)
+    assert np.array_equal(N(idx).view(np.uint32), si)
+    assert np.array_equal(N(keys).view(sk.dtype), sk)
+
+
+def test_sort_scratch_too_small(wf, dev):
+    import torch
+    k = torch.zeros(5000, dtype=torch.int32, device=dev)
+    v = torch.zeros(5000, dtype=torch.int32, device=dev)
+    small = torch.empty(64, dtype=torch.uint8, device=dev)
+    with pytest.raises(wf.WfptError):
+        wf.api.sort_pairs(k, v, 32, scratch=small)

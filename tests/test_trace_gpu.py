@@ -1,0 +1,146 @@
+"""Traversal through the C ABI.
+
+Plain form (BVH2 FP32) is bit-exact against the oracle's CPU traversal of
+the same BVH; the chosen form (BVH8 with 8-bit boxes) returns the same
+closest hits as the plain form (same watertight test and tie rule); both
+agree with the FP64 oracle: primitive ids except at ties, hit distance
+within 1e-5 relative or 1e-6 of the scene scale (the FP32 coordinate floor).
+"""
+import numpy as np
+import pytest
+
+from conftest import random_rays
+
+pytestmark = pytest.mark.gpu
+
+
+def T(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def N(t):
+    return t.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def soup(wf):
+    pos, nrm, idx = wf.api.generate_scene(0, 1, 65536)
+    sc = wf.api.Scene(pos, idx)
+    return pos, idx, sc
+
+
+@pytest.fixture(scope="module")
+def courtyard(wf):
+    pos, nrm, idx = wf.api.generate_scene(1, 1)
+    sc = wf.api.Scene(pos, idx)
+    return pos, idx, sc
+
+
+def gpu_trace(wf, dev, sc, kind, rays, closest=True, ray_index=None):
+    import torch
+    out = torch.full((rays.shape[0], 4), 77, dtype=torch.int32, device=dev)
+    wf.api.trace(sc, kind, T(rays, dev), out, ray_index=None if ray_index is None else T(ray_index, dev),
+                 closest_hit=closest)
+    return N(out)
+
+
+def test_bvh2_bit_exact_vs_cpu_traversal(wf, orc, dev, soup):
+    pos, idx, sc = soup
+    nodes, tris = sc.export_bvh2()
+    rays = random_rays(np.random.default_rng(2), 200000)
+    g = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
+    c = orc.trace_bvh2(nodes, tris, rays)
+    assert np.array_equal(g, c)
+    ga = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=False)
+    ca = orc.trace_bvh2(nodes, tris, rays, closest=False)
+    assert np.array_equal(ga, ca)
+    assert wf.api.device_status() == 0
+
+
+@pytest.mark.parametrize("scene", ["soup", "courtyard"])
+def test_bvh8_equals_bvh2(wf, dev, scene, request):
+    pos, idx, sc = request.getfixturevalue(scene)
+    lo, hi = sc.bounds_min, sc.bounds_max
+    rng = np.random.default_rng(3)
+    n = 300000
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    rays = random_rays(rng, n, tmax=1e30)
+    rays[:, :3] = o
+    g2 = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
+    g8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays)
+    assert np.array_equal(g2, g8)
+    a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)
+    assert np.array_equal(a8[:, 0] >= 0, g2[:, 0] >= 0)
+    assert wf.api.device_status() == 0
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_against_fp64(wf, orc, dev, soup, kind):
+    pos, idx, sc = soup
+    rays = random_rays(np.random.default_rng(5 + kind), 100000)
+    g = gpu_trace(wf, dev, sc, kind, rays)
+    t64, tri64 = orc.Fp64Scene(pos, idx).trace(rays)
+    hit = g[:, 0] >= 0
+    assert np.mean(hit == (tri64 >= 0)) > 0.9999
+    both = hit & (tri64 >= 0)
+    assert np.mean(g[both, 0] == tri64[both]) > 0.9999
+    t32 = g[both, 2].view(np.float32).astype(np.float64)
+    assert np.all(np.abs(t32 - t64[both]) <= 1e-5 * t64[both] + 1e-6)
+
+
+def test_indirect_index_and_empty_interval(wf, dev, soup):
+    pos, idx, sc = soup
+    rng = np.random.default_rng(8)
+    rays = random_rays(rng, 50000)
+    rays[::9, 7] = -1.0  # tmax < tmin: miss (raygenShadow.comp:129 dummy rays)
+    direct = gpu_trace(wf, dev, sc, 1, rays)
+    assert np.all(direct[::9, 0] == -1) and np.all(direct[::9, 2].view(np.float32) == -1.0)
+    perm = rng.permutation(50000).astype(np.uint32)
+    ind = gpu_trace(wf, dev, sc, 1, rays, ray_index=perm.view(np.int32))
+    assert np.array_equal(ind, direct)
+
+
+def test_miss_record_and_device_count(wf, dev, soup):
+    import torch
+    pos, idx, sc = soup
+    rays = random_rays(np.random.default_rng(1), 1000)
+    rays[:, :3] += 10.0  # outside the scene, pointing anywhere: mostly misses
+    out = torch.full((1000, 4), 5, dtype=torch.int32, device=dev)
+    cnt = torch.tensor([600], dtype=torch.int32, device=dev)
+    wf.api.trace(sc, 1, T(rays, dev), out, n_dev=cnt)
+    o = N(out)
+    miss = o[:600, 0] == -1
+    assert np.all(o[:600][miss][:, 1] == -1) and np.all(o[:600][miss][:, 3] == 0)
+    assert np.all(o[600:] == 5)
+
+
+def test_empty_and_tiny_scenes(wf, dev):
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    idx = np.array([[0, 1, 2]], np.uint32)
+    sc = wf.api.Scene(pos, idx)
+    rays = np.zeros((2, 8), np.float32)
+    rays[:, :3] = [[0.2, 0.2, 1.0], [2.0, 2.0, 1.0]]
+    rays[:, 6] = -1.0
+    rays[:, 7] = 10.0
+    for kind in (0, 1):
+        o = gpu_trace(wf, dev, sc, kind, rays)
+        assert o[0, 0] == 0 and o[0, 1] == 0 and abs(o[0, 2].view(np.float32) - 1.0) < 1e-6
+        u, v = (o[0, 3] & 0xFFFF) / 65535.0, (o[0, 3] >> 16) / 65535.0
+        assert abs(u - 0.2) < 1e-4 and abs(v - 0.2) < 1e-4
+        assert o[1, 0] == -1
+    empty = wf.api.Scene(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    for kind in (0, 1):
+        assert np.all(gpu_trace(wf, dev, empty, kind, rays)[:, 0] == -1)
+
+
+def test_multi_geometry_ids(wf, dev):
+    pos, nrm, idx = wf.api.generate_scene(0, 3, 3000)
+    sc = wf.api.Scene(pos, idx, geometry_first=[0, 1000, 2500])
+    rays = random_rays(np.random.default_rng(4), 20000)
+    o = gpu_trace(wf, dev, sc, 1, rays)
+    hit = o[o[:, 0] >= 0]
+    glob = np.where(hit[:, 1] == 0, hit[:, 0], np.where(hit[:, 1] == 1, hit[:, 0] + 1000, hit[:, 0] + 2500))
+    assert np.all((glob >= 0) & (glob < 3000))
+    assert set(np.unique(hit[:, 1])) <= {0, 1, 2}
+    assert np.all(hit[hit[:, 1] == 1, 0] < 1500) and np.all(hit[hit[:, 1] == 2, 0] < 500)

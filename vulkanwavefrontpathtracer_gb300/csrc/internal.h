@@ -1,0 +1,23 @@
+// Host-only internals shared by the C ABI translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/wfpt.h"
+#include "scene.h"
+
+namespace wfpt {
+
+// Device status word bits (kErrTimeout / kErrBounds in common.cuh).
+constexpr uint32_t kStatusTimeout = 1u;
+constexpr uint32_t kStatusBounds = 2u;
+
+wfpt_status from_cuda(cudaError_t e);
+void set_error(const char* msg);
+
+const SceneDevice* scene_device(const wfpt_scene* s);
+bool scene_has(const wfpt_scene* s, int kind);
+void scene_bounds(const wfpt_scene* s, float mn[3], float mx[3]);
+
+}  // namespace wfpt

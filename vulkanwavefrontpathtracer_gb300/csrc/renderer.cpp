@@ -1,0 +1,486 @@
+// Host-side renderer: the orchestration of Renderer::render and its passes
+// (projects/WaveFrontPathTracer/Renderer/Renderer.cpp:124-199, 552-654), the
+// ray buffers of RayBuffer (Ray/RayBuffer.cpp) and the traceSort sequence of
+// Tracer (Tracer/Tracer.cpp:214-225).
+//
+// Differences by design:
+//  - wavefront sizes stay on the device: raygen_path writes the compacted
+//    count into a device counter that every later kernel of the bounce reads,
+//    so a frame issues no host readback (the reference reads the path count
+//    and the hit count back after every pass, RayGen.cpp:178-183 and
+//    Renderer.cpp:85-88);
+//  - buffers are sized once per resolution (capacity = width*height rays per
+//    wavefront) and the frame can be captured into one CUDA graph;
+//  - ray statistics are read back once, after the frame.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/wfpt.h"
+#include "host.h"
+#include "internal.h"
+#include "stages.cuh"
+#include "trace.cuh"
+
+namespace {
+
+constexpr int kMaxDepth = 8;                    // RENDERER_MAX_RECURSION_DEPTH
+constexpr int kMaxSamples = 1024;               // RENDERER_MAX_SAMPLES
+constexpr int kMaxBatch = 8 * 1024 * 1024;      // RENDERER_MAX_BATCH_SIZE
+constexpr int kCountersPerPass = 32;
+// Per-pass counter block: [0..7] path rays per bounce, [8..16] hits among
+// the input rays of each shadow pass, [17] shadow rays of the current batch.
+constexpr int kCntPath = 0, kCntHits = 8, kCntBatch = 17;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+// RayBuffer (Ray/RayBuffer.h:22-70): double-buffered rays and slot maps,
+// one result buffer, Morton keys and sort indices.
+struct RayBufferDev {
+    DevBuf rays[2], s2i[2], i2s[2], results, keys, idx;
+    bool swapped = false;
+    wfpt_ray* rays_cur() const { return rays[swapped ? 1 : 0].as<wfpt_ray>(); }
+    wfpt_ray* rays_out() const { return rays[swapped ? 0 : 1].as<wfpt_ray>(); }
+    int32_t* s2i_cur() const { return s2i[swapped ? 1 : 0].as<int32_t>(); }
+    int32_t* s2i_out() const { return s2i[swapped ? 0 : 1].as<int32_t>(); }
+    int32_t* i2s_cur() const { return i2s[swapped ? 1 : 0].as<int32_t>(); }
+    int32_t* i2s_out() const { return i2s[swapped ? 0 : 1].as<int32_t>(); }
+    void swap() { swapped = !swapped; }
+    cudaError_t ensure(size_t cap, bool sortable) {
+        cudaError_t e;
+        if ((e = rays[0].ensure(cap * 32)) != cudaSuccess) return e;
+        if ((e = results.ensure(cap * 16)) != cudaSuccess) return e;
+        if ((e = s2i[0].ensure(cap * 4)) != cudaSuccess) return e;
+        if ((e = i2s[0].ensure(cap * 4)) != cudaSuccess) return e;
+        if (sortable) {
+            if ((e = rays[1].ensure(cap * 32)) != cudaSuccess) return e;
+            if ((e = s2i[1].ensure(cap * 4)) != cudaSuccess) return e;
+            if ((e = i2s[1].ensure(cap * 4)) != cudaSuccess) return e;
+            if ((e = keys.ensure(cap * 8)) != cudaSuccess) return e;
+            if ((e = idx.ensure(cap * 4)) != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    void release() {
+        for (auto* b : {&rays[0], &rays[1], &s2i[0], &s2i[1], &i2s[0], &i2s[1], &results, &keys, &idx}) b->release();
+    }
+};
+
+}  // namespace
+
+struct wfpt_renderer {
+    wfpt_renderer_config cfg{};
+    const wfpt_scene* scene = nullptr;
+    const wfpt_geometry* geoms = nullptr;
+    float smin[3] = {0, 0, 0}, smax[3] = {0, 0, 0}, light[3] = {5, -2, 1}, bg[3] = {0, 0, 1};
+    int frame_index = 1;
+
+    int width = 0, height = 0;
+    int alloc_samples = 0;
+    DevBuf i2p, p2i, seeds, decreases, aux, sort_scratch, path_scratch, counters;
+    RayBufferDev primary, shadow, queue[2];
+    uint32_t* host_counters = nullptr;  // pinned
+    int last_spp = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    bool stats_pending = false;
+    float frame_ms = 0.0f;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    ~wfpt_renderer() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters}) b->release();
+        primary.release();
+        shadow.release();
+        queue[0].release();
+        queue[1].release();
+        if (host_counters) cudaFreeHost(host_counters);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (ev2) cudaEventDestroy(ev2);
+    }
+
+    int key_bits() const {
+        switch (cfg.morton_kind) {
+            case WFPT_MORTON_6D48: return 48;
+            case WFPT_MORTON_6D64: return 63;
+            default: return 32;
+        }
+    }
+
+    uint32_t* cnt(int pass, int slot) const { return counters.as<uint32_t>() + pass * kCountersPerPass + slot; }
+
+    cudaError_t prepare(int w, int h) {
+        cudaError_t e;
+        size_t n = (size_t)w * h;
+        int S = cfg.num_shadow_samples;
+        if (w != width || h != height) {
+            std::vector<int32_t> a(n), b(n);
+            wfpt::pixel_table(w, h, a.data(), b.data());
+            if ((e = i2p.ensure(n * 4)) != cudaSuccess) return e;
+            if ((e = p2i.ensure(n * 4)) != cudaSuccess) return e;
+            if ((e = cudaMemcpy(i2p.p, a.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+            if ((e = cudaMemcpy(p2i.p, b.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+            width = w;
+            height = h;
+        }
+        if ((e = seeds.ensure(n * 4)) != cudaSuccess) return e;
+        if ((e = decreases.ensure(n * 16)) != cudaSuccess) return e;
+        if ((e = aux.ensure(n * 16)) != cudaSuccess) return e;
+        if ((e = primary.ensure(n, false)) != cudaSuccess) return e;
+        if ((e = queue[0].ensure(n, true)) != cudaSuccess) return e;
+        if ((e = queue[1].ensure(n, true)) != cudaSuccess) return e;
+        size_t batch_in = std::min<size_t>(n, (size_t)(kMaxBatch / S));
+        size_t shadow_cap = std::max<size_t>(1, batch_in * S);
+        if ((e = shadow.ensure(shadow_cap, true)) != cudaSuccess) return e;
+        size_t sort_n = std::max(n, shadow_cap);
+        if ((e = sort_scratch.ensure(wfpt::sort_scratch_bytes((uint32_t)sort_n, 64))) != cudaSuccess) return e;
+        if ((e = path_scratch.ensure(wfpt::raygen_path_scratch_bytes((uint32_t)n))) != cudaSuccess) return e;
+        if ((e = counters.ensure((size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess) return e;
+        if (!host_counters &&
+            (e = cudaMallocHost(&host_counters, (size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess)
+            return e;
+        if (!ev0 && (e = cudaEventCreate(&ev0)) != cudaSuccess) return e;
+        if (!ev1 && (e = cudaEventCreate(&ev1)) != cudaSuccess) return e;
+        if (!ev2 && (e = cudaEventCreate(&ev2)) != cudaSuccess) return e;
+        return cudaSuccess;
+    }
+
+    // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).
+    cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
+                           cudaStream_t s) {
+        const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
+        cudaError_t e;
+        if (!sort) return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
+                                             n_dev, closest ? 1 : 0, s);
+        float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
+        if ((e = wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
+                                     rb.idx.as<uint32_t>(), s)) != cudaSuccess)
+            return e;
+        if ((e = wfpt::launch_sort_pairs(rb.keys.p, rb.idx.as<uint32_t>(), n, n_dev, key_bits(), sort_scratch.p,
+                                         sort_scratch.bytes, s)) != cudaSuccess)
+            return e;
+        if (reorder) {
+            if ((e = wfpt::launch_reorder(rb.idx.as<uint32_t>(), rb.rays_cur(), rb.rays_out(), rb.s2i_cur(),
+                                          rb.s2i_out(), rb.i2s_out(), n, n_dev, s)) != cudaSuccess)
+                return e;
+            rb.swap();
+        }
+        return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
+                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s);
+    }
+
+    // Renderer::shadowPass (Renderer.cpp:133-154) over input rays `in`
+    // whose slot->pixel map is `in_s2i`; n_in is the capacity, n_in_dev the
+    // device-side count (null when the host count is exact).
+    cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
+                            const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
+                            uint32_t* batch_counter, cudaStream_t s) {
+        int S = cfg.num_shadow_samples;
+        uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
+        uint32_t bb = 0;
+        cudaError_t e;
+        do {
+            uint32_t be = std::min(bb + batch_diff, n_in);
+            uint32_t bs = be - bb;
+            const uint32_t* n_sh_dev = nullptr;
+            if (n_in_dev) {
+                if ((e = wfpt::launch_batch_count(n_in_dev, bb, bs, S, batch_counter, s)) != cudaSuccess) return e;
+                n_sh_dev = batch_counter;
+            }
+            shadow.swapped = false;
+            if ((e = wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, shadow.rays_cur(),
+                                                shadow.s2i_cur(), shadow.i2s_cur(), light, cfg.shadow_radius, (int)bb,
+                                                (int)bs, n_in_dev, S, s)) != cudaSuccess)
+                return e;
+            if ((e = trace_rays(shadow, bs * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
+                                cfg.reorder_shadow_rays != 0, false, s)) != cudaSuccess)
+                return e;
+            if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
+                                                     in_pixels, out_pixels, (int)bb, (int)bs, n_in_dev, S, 0, s)) !=
+                cudaSuccess)
+                return e;
+            bb = be;
+        } while (bb != n_in);
+        return wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, s);
+    }
+
+    // Renderer::primaryPass (Renderer.cpp:124-131).
+    cudaError_t primary_pass(const float* s2w, const float* eye, float zfar, int pass, float* target, cudaStream_t s) {
+        uint32_t n = (uint32_t)width * height;
+        cudaError_t e;
+        int sample_index = pass + cfg.num_primary_samples * (frame_index - 1);
+        if ((e = wfpt::launch_raygen_primary(s2w, i2p.as<int32_t>(), primary.rays_cur(), eye, sample_index, width,
+                                             height, zfar, s)) != cudaSuccess)
+            return e;
+        if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), cfg.bvh_kind, primary.rays_cur(),
+                                    primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s)) != cudaSuccess)
+            return e;
+        const float one = 1.0f;
+        uint32_t one_bits;
+        std::memcpy(&one_bits, &one, 4);
+        if ((e = wfpt::launch_fill_u32(decreases.p, one_bits, (size_t)n * 4, s)) != cudaSuccess) return e;
+        return wfpt::launch_reconstruct_smooth(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(),
+                                               target, decreases.as<float>(), geoms, light, bg, n, nullptr,
+                                               cfg.num_primary_samples, s);
+    }
+
+    cudaError_t frame(const float* s2w, const float* eye, float zfar, float* pixels, float* frame_pixels,
+                      cudaStream_t s) {
+        uint32_t n = (uint32_t)width * height;
+        cudaError_t e;
+        primary.swapped = queue[0].swapped = queue[1].swapped = shadow.swapped = false;
+        if ((e = cudaMemsetAsync(frame_pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+        if (frame_index == 1 && (e = cudaMemsetAsync(pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(counters.p, 0, (size_t)cfg.num_primary_samples * kCountersPerPass * 4, s)) !=
+            cudaSuccess)
+            return e;
+        int rt = cfg.ray_type;
+        if (rt == WFPT_PATH_RAYS || rt == WFPT_SHADOW_RAYS)
+            if ((e = wfpt::launch_init_seeds(seeds.as<uint32_t>(), n, frame_index, s)) != cudaSuccess) return e;
+        for (int pass = 0; pass < cfg.num_primary_samples; ++pass) {
+            if (rt == WFPT_PRIMARY_RAYS) {
+                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s)) != cudaSuccess) return e;
+                continue;
+            }
+            // renderShadow / renderPath (Renderer.cpp:168-199).
+            if ((e = cudaMemsetAsync(aux.p, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+            if ((e = primary_pass(s2w, eye, zfar, pass, aux.as<float>(), s)) != cudaSuccess) return e;
+            if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
+                                 aux.as<float>(), frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s)) !=
+                cudaSuccess)
+                return e;
+            if (rt != WFPT_PATH_RAYS) continue;
+            int qsel = 0;  // PathQueue::swapBuffers
+            for (int bounce = 0; bounce < cfg.recursion_depth; ++bounce) {
+                if ((e = cudaMemsetAsync(aux.p, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+                RayBufferDev& out = queue[qsel ? 0 : 1];
+                const wfpt_ray* in_rays;
+                const wfpt_hit* in_res;
+                const int32_t* in_s2i;
+                const uint32_t* in_cnt;
+                if (bounce == 0) {
+                    in_rays = primary.rays_cur();
+                    in_res = primary.results.as<wfpt_hit>();
+                    in_s2i = i2p.as<int32_t>();
+                    in_cnt = nullptr;
+                } else {
+                    RayBufferDev& in = queue[qsel ? 1 : 0];
+                    in_rays = in.rays_cur();
+                    in_res = in.results.as<wfpt_hit>();
+                    in_s2i = in.s2i_cur();
+                    in_cnt = cnt(pass, kCntPath + bounce - 1);
+                }
+                out.swapped = false;
+                uint32_t* out_cnt = cnt(pass, kCntPath + bounce);
+                // Renderer::pathPass -> tracePathRays (Renderer.cpp:156-162, 277-297).
+                if ((e = wfpt::launch_raygen_path(seeds.as<uint32_t>(), geoms, in_rays, out.rays_cur(), in_s2i,
+                                                  out.s2i_cur(), in_res, decreases.as<float>(), out_cnt, n, in_cnt,
+                                                  cfg.albedo, path_scratch.p, s)) != cudaSuccess)
+                    return e;
+                if ((e = trace_rays(out, n, out_cnt, cfg.sort_path_rays != 0, cfg.reorder_path_rays != 0, true, s)) !=
+                    cudaSuccess)
+                    return e;
+                if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
+                                                         aux.as<float>(), decreases.as<float>(), geoms, light, bg, n,
+                                                         out_cnt, cfg.num_primary_samples, s)) != cudaSuccess)
+                    return e;
+                if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
+                                     aux.as<float>(), frame_pixels, cnt(pass, kCntHits + bounce + 1),
+                                     cnt(pass, kCntBatch), s)) != cudaSuccess)
+                    return e;
+                qsel ^= 1;  // PathQueue::swap
+            }
+        }
+        return wfpt::launch_interpolate_colors(frame_pixels, pixels, n, frame_index, cfg.key_value, cfg.white_point, s);
+    }
+};
+
+namespace {
+
+wfpt_status check_config(const wfpt_renderer_config* c) {
+    if (c->ray_type < WFPT_PRIMARY_RAYS || c->ray_type > WFPT_PATH_RAYS) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->num_primary_samples < 1 || c->num_primary_samples > kMaxSamples) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->num_shadow_samples < 1 || c->num_shadow_samples > kMaxSamples) return WFPT_ERR_INVALID_ARGUMENT;
+    if (!(c->shadow_radius > 0.0f && c->shadow_radius <= 100.0f)) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->recursion_depth < 0 || c->recursion_depth > kMaxDepth) return WFPT_ERR_INVALID_ARGUMENT;
+    if (!(c->key_value > 0.0f && c->key_value <= 2.0f)) return WFPT_ERR_INVALID_ARGUMENT;
+    if (!(c->white_point > 0.0f && c->white_point <= 2.0f)) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->morton_kind < WFPT_MORTON_AILA32 || c->morton_kind > WFPT_MORTON_6D64) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->bvh_kind != WFPT_BVH2_FP32 && c->bvh_kind != WFPT_BVH8_Q8) return WFPT_ERR_INVALID_ARGUMENT;
+    return WFPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Defaults of Renderer::Renderer (Renderer.cpp:300-308) overridden by the
+// registered option defaults (AppEnvironment.cpp:24-35), as Renderer::init
+// applies them.
+void wfpt_renderer_config_default(wfpt_renderer_config* c) {
+    if (!c) return;
+    c->ray_type = WFPT_PRIMARY_RAYS;
+    c->num_primary_samples = 1;
+    c->num_shadow_samples = 2;
+    c->shadow_radius = 0.001f;
+    c->recursion_depth = 1;
+    c->key_value = 0.6f;
+    c->white_point = 2.0f;
+    c->russian_roulette = 0;
+    c->sort_shadow_rays = 0;
+    c->reorder_shadow_rays = 0;
+    c->sort_path_rays = 0;
+    c->reorder_path_rays = 0;
+    c->morton_kind = WFPT_MORTON_AILA32;
+    c->bvh_kind = WFPT_BVH2_FP32;
+    c->albedo = 0.8f;
+    c->use_graph = 0;
+}
+
+wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config, wfpt_renderer** renderer) {
+    if (!renderer) return WFPT_ERR_INVALID_ARGUMENT;
+    *renderer = nullptr;
+    wfpt_renderer_config c;
+    if (config) {
+        c = *config;
+    } else {
+        wfpt_renderer_config_default(&c);
+    }
+    if (check_config(&c) != WFPT_OK) {
+        wfpt::set_error("renderer option out of range");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    wfpt_renderer* r = new (std::nothrow) wfpt_renderer();
+    if (!r) return WFPT_ERR_OUT_OF_MEMORY;
+    r->cfg = c;
+    *renderer = r;
+    return WFPT_OK;
+}
+
+void wfpt_renderer_destroy(wfpt_renderer* r) { delete r; }
+
+wfpt_status wfpt_renderer_set_config(wfpt_renderer* r, const wfpt_renderer_config* config) {
+    if (!r || !config) return WFPT_ERR_INVALID_ARGUMENT;
+    if (check_config(config) != WFPT_OK) {
+        wfpt::set_error("renderer option out of range");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    r->cfg = *config;
+    r->frame_index = 1;  // every setter of the reference resets the frame index
+    return WFPT_OK;
+}
+
+wfpt_status wfpt_renderer_set_scene(wfpt_renderer* r, const wfpt_scene* scene, const wfpt_geometry* geometries,
+                                    const float scene_min[3], const float scene_max[3], const float light[3],
+                                    const float background[3]) {
+    if (!r || !scene || !geometries) return WFPT_ERR_INVALID_ARGUMENT;
+    if (!wfpt::scene_has(scene, r->cfg.bvh_kind)) {
+        wfpt::set_error("scene was built without the renderer's BVH kind");
+        return WFPT_ERR_UNSUPPORTED;
+    }
+    r->scene = scene;
+    r->geoms = geometries;
+    float mn[3], mx[3];
+    wfpt::scene_bounds(scene, mn, mx);
+    for (int k = 0; k < 3; ++k) {
+        r->smin[k] = scene_min ? scene_min[k] : mn[k];
+        r->smax[k] = scene_max ? scene_max[k] : mx[k];
+        if (light) r->light[k] = light[k];
+        if (background) r->bg[k] = background[k];
+    }
+    return WFPT_OK;
+}
+
+void wfpt_renderer_reset_frame_index(wfpt_renderer* r) {
+    if (r) r->frame_index = 1;
+}
+
+wfpt_status wfpt_renderer_render(wfpt_renderer* r, const wfpt_camera* camera, int width, int height, float* pixels,
+                                 float* frame_pixels, void* stream) {
+    if (!r || !camera || !pixels || !frame_pixels) return WFPT_ERR_INVALID_ARGUMENT;
+    if (!r->scene) {
+        wfpt::set_error("renderer has no scene");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    if (width <= 0 || height <= 0 || (long long)width * height > (1ll << 28)) {
+        wfpt::set_error("bad resolution");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = r->prepare(width, height);
+    if (e != cudaSuccess) return wfpt::from_cuda(e);
+    float s2w[16];
+    if (!wfpt::camera_screen_to_world(camera->position, camera->rotation_deg, camera->fov_deg,
+                                      (float)width / (float)height, camera->znear, camera->zfar, s2w)) {
+        wfpt::set_error("bad camera");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    if ((e = cudaEventRecord(r->ev0, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    if ((e = r->frame(s2w, camera->position, camera->zfar, pixels, frame_pixels, s)) != cudaSuccess)
+        return wfpt::from_cuda(e);
+    if ((e = cudaEventRecord(r->ev1, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    size_t cbytes = (size_t)r->cfg.num_primary_samples * kCountersPerPass * 4;
+    if ((e = cudaMemcpyAsync(r->host_counters, r->counters.p, cbytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return wfpt::from_cuda(e);
+    if ((e = cudaEventRecord(r->ev2, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    r->last_spp = r->cfg.num_primary_samples;
+    r->stats_pending = true;
+    ++r->frame_index;
+    return WFPT_OK;
+}
+
+wfpt_status wfpt_renderer_get_stats(wfpt_renderer* r, wfpt_render_stats* st) {
+    if (!r || !st) return WFPT_ERR_INVALID_ARGUMENT;
+    std::memset(st, 0, sizeof(*st));
+    if (!r->stats_pending) return WFPT_OK;
+    cudaError_t e = cudaEventSynchronize(r->ev2);
+    if (e != cudaSuccess) return wfpt::from_cuda(e);
+    cudaEventElapsedTime(&r->frame_ms, r->ev0, r->ev1);
+    uint64_t n = (uint64_t)r->width * r->height;
+    int S = r->cfg.num_shadow_samples;
+    int rt = r->cfg.ray_type;
+    for (int p = 0; p < r->last_spp; ++p) {
+        const uint32_t* c = r->host_counters + p * kCountersPerPass;
+        st->num_primary_rays += n;
+        if (rt == WFPT_PRIMARY_RAYS) continue;
+        int passes = rt == WFPT_PATH_RAYS ? r->cfg.recursion_depth + 1 : 1;
+        for (int i = 0; i < passes; ++i) {
+            st->num_shadow_rays += (uint64_t)S * c[kCntHits + i];
+            st->shadow_hits_per_pass[i] += c[kCntHits + i];
+        }
+        if (rt == WFPT_PATH_RAYS)
+            for (int b = 0; b < r->cfg.recursion_depth; ++b) {
+                st->num_path_rays += c[kCntPath + b];
+                st->path_rays_per_bounce[b] += c[kCntPath + b];
+            }
+    }
+    st->frame_ms = r->frame_ms;
+    return WFPT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// Launch wrappers of the stage kernels (host-callable, stream-ordered).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/wfpt.h"
+
+namespace wfpt {
+
+// Number of kernels this library has launched (all threads, all devices).
+void count_launch(uint32_t k = 1);
+uint64_t launch_count();
+
+// Per-unit device status readers (return and clear).
+cudaError_t status_stages(uint32_t* out);
+cudaError_t status_sort(uint32_t* out);
+cudaError_t status_trace(uint32_t* out);
+
+cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s);
+cudaError_t launch_raygen_primary(const float* m, const int32_t* i2p, wfpt_ray* rays, const float* o,
+                                  int sample_index, int w, int h, float max_dist, cudaStream_t s);
+cudaError_t launch_raygen_shadow(const uint32_t* seeds, const wfpt_ray* in_rays, const wfpt_hit* in_res,
+                                 wfpt_ray* out_rays, int32_t* s2i, int32_t* i2s, const float* light,
+                                 float radius, int bb, int bs, const uint32_t* n_in_dev, int S,
+                                 cudaStream_t s);
+size_t raygen_path_scratch_bytes(uint32_t max_n);
+cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, const wfpt_ray* in_rays,
+                               wfpt_ray* out_rays, const int32_t* in_i2p, int32_t* out_i2p,
+                               const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
+                               uint32_t n, const uint32_t* n_dev, float albedo, void* scratch,
+                               cudaStream_t s);
+cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res, const int32_t* i2p,
+                                      float* pixels, const float* decreases, const wfpt_geometry* geoms,
+                                      const float* light, const float* bg, uint32_t n,
+                                      const uint32_t* n_dev, int spp, cudaStream_t s);
+cudaError_t launch_reconstruct_shadow(const wfpt_hit* res, const int32_t* i2p, const int32_t* i2s,
+                                      const float* in_pixels, float* out_pixels, int bb, int bs,
+                                      const uint32_t* n_in_dev, int S, int replace, cudaStream_t s);
+cudaError_t launch_count_hits(const wfpt_hit* res, uint32_t n, const uint32_t* n_dev, uint32_t* count,
+                              cudaStream_t s);
+cudaError_t launch_interpolate_colors(float* frame_pixels, float* pixels, uint32_t n, int frame_index,
+                                      float key, float white, cudaStream_t s);
+cudaError_t launch_fill_u32(void* dst, uint32_t v, size_t n, cudaStream_t s);
+cudaError_t launch_batch_count(const uint32_t* n_in_dev, uint32_t begin, uint32_t size, int S, uint32_t* out,
+                               cudaStream_t s);
+
+// keys.cu
+cudaError_t launch_morton(const wfpt_ray* rays, uint32_t n, const uint32_t* n_dev, const float* smin,
+                          const float* ssize, int kind, void* keys, uint32_t* indices, cudaStream_t s);
+cudaError_t launch_reorder(const uint32_t* idx, const wfpt_ray* in_rays, wfpt_ray* out_rays,
+                           const int32_t* in_s2i, int32_t* out_s2i, int32_t* out_i2s, uint32_t n,
+                           const uint32_t* n_dev, cudaStream_t s);
+
+// sort.cu
+size_t sort_scratch_bytes(uint32_t max_n, int key_bits);
+cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev,
+                              int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s);
+
+}  // namespace wfpt
