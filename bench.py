@@ -9,7 +9,7 @@ Morton keys, radix sort, reorder and traversal, shading, accumulation.
 
 Forms:
   chosen  8-wide BVH with 8-bit quantised boxes, 64-bit 6-D Morton keys,
-          sort + reorder of path and shadow rays
+          sort + reorder of the path rays of every bounce
   plain   binary BVH with FP32 boxes, no sorting
 The headline value is the chosen form's rays per second over the whole
 frame (reference metric Mrays/s = rays * 1e-3 / ms, Renderer.cpp:692-706,
@@ -43,12 +43,14 @@ COURTYARD = dict(
     renderer=dict(ray_type=2, num_primary_samples=1, num_shadow_samples=2, shadow_radius=1.0, recursion_depth=8,
                   key_value=0.6, white_point=2.0, albedo=0.8),
 )
-CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1,
-              reorder_shadow_rays=1)
+# Shadow rays are generated in the (already reordered) slot order of their
+# path rays and all aim at the light, so the chosen form does not sort them.
+CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=0,
+              reorder_shadow_rays=0)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
              reorder_shadow_rays=0)
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
-                 "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path and shadow rays")
+                 "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
 
 
@@ -324,6 +326,24 @@ def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
     }
 
 
+def run_micro_only(args):
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    dev = torch.device("cuda", 0)
+    api = wf.api
+    W = COURTYARD
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx)
+    geom = api.Geometry(pos, nrm, idx, device=dev)
+    cam = api.make_camera(**W["camera"])
+    micro = bounce_micro(wf, api, dev, scene, geom, cam, args.width, args.height, torch.cuda.current_stream())
+    print(json.dumps({"micro": micro["per_bounce"], "sort_gbs": round(micro["sort"]["gbs"], 1),
+                      "reorder_gbs": round(micro["reorder"]["gbs"], 1), "resolution": [args.width, args.height]}))
+
+
 # ---------------------------------------------------------- CPU baseline
 def cpu_frame(args, api, scene, pos, nrm, idx, w, h, form):
     import oracle
@@ -397,7 +417,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--micro-only", action="store_true",
+                    help="only the bounce-1 microbenchmark (small profiling case with --width/--height)")
+    ap.add_argument("--width", type=int, default=COURTYARD["width"])
+    ap.add_argument("--height", type=int, default=COURTYARD["height"])
     args = ap.parse_args()
+    if args.micro_only:
+        run_micro_only(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -49,31 +49,47 @@ def _f(v, n):
     return a
 
 
+_KEEP: list = []
+
+
 def ptr(a: np.ndarray):
-    return C.c_void_p(a.ctypes.data) if a is not None else None
+    """Pointer to a numpy array; the array is kept alive until the next
+    oracle call returns (temporaries passed inline would otherwise be freed
+    before the C function runs)."""
+    if a is None:
+        return None
+    _KEEP.append(a)
+    return C.c_void_p(a.ctypes.data)
+
+
+def _call(fn, *args):
+    try:
+        return fn(*args)
+    finally:
+        _KEEP.clear()
 
 
 def num_threads() -> int:
-    return load().orc_num_threads()
+    return _call(load().orc_num_threads, )
 
 
 def init_seeds(n, frame_index):
     s = np.empty(n, np.uint32)
-    load().orc_init_seeds(ptr(s), C.c_uint32(n), C.c_int(frame_index))
+    _call(load().orc_init_seeds, ptr(s), C.c_uint32(n), C.c_int(frame_index))
     return s
 
 
 def pixel_table(w, h):
     a = np.empty(w * h, np.int32)
     b = np.empty(w * h, np.int32)
-    load().orc_pixel_table(C.c_int(w), C.c_int(h), ptr(a), ptr(b))
+    _call(load().orc_pixel_table, C.c_int(w), C.c_int(h), ptr(a), ptr(b))
     return a, b
 
 
 def camera_screen_to_world(pos, rot, fov, aspect, zn, zf):
     out = np.empty(16, np.float32)
     p, r = _f(pos, 3), _f(rot, 3)
-    load().orc_camera_screen_to_world(ptr(p), ptr(r), C.c_float(fov), C.c_float(aspect), C.c_float(zn),
+    _call(load().orc_camera_screen_to_world, ptr(p), ptr(r), C.c_float(fov), C.c_float(aspect), C.c_float(zn),
                                       C.c_float(zf), ptr(out))
     return out
 
@@ -82,7 +98,7 @@ def raygen_primary(m, i2p, origin, sample_index, w, h, max_dist):
     rays = np.empty((w * h, 8), np.float32)
     m, o = _f(m, 16), _f(origin, 3)
     i2p = np.ascontiguousarray(i2p, np.int32)
-    load().orc_raygen_primary(ptr(m), ptr(i2p), ptr(rays), ptr(o), C.c_int(sample_index), C.c_int(w), C.c_int(h),
+    _call(load().orc_raygen_primary, ptr(m), ptr(i2p), ptr(rays), ptr(o), C.c_int(sample_index), C.c_int(w), C.c_int(h),
                               C.c_float(max_dist))
     return rays
 
@@ -93,14 +109,14 @@ def morton(rays, smin, ssize, kind):
     keys = np.empty(n, np.uint32 if kind == 0 else np.uint64)
     idx = np.empty(n, np.uint32)
     a, b = _f(smin, 3), _f(ssize, 3)
-    load().orc_morton(ptr(rays), C.c_uint32(n), ptr(a), ptr(b), C.c_int(kind), ptr(keys), ptr(idx))
+    _call(load().orc_morton, ptr(rays), C.c_uint32(n), ptr(a), ptr(b), C.c_int(kind), ptr(keys), ptr(idx))
     return keys, idx
 
 
 def sort_pairs(keys, vals, key_bits):
     keys = np.ascontiguousarray(keys).copy()
     vals = np.ascontiguousarray(vals, np.uint32).copy()
-    load().orc_sort_pairs(ptr(keys), ptr(vals), C.c_uint32(keys.shape[0]), C.c_int(key_bits))
+    _call(load().orc_sort_pairs, ptr(keys), ptr(vals), C.c_uint32(keys.shape[0]), C.c_int(key_bits))
     return keys, vals
 
 
@@ -109,20 +125,20 @@ def reorder(idx, in_rays, in_s2i, index_space=None):
     out = np.empty((n, 8), np.float32)
     s2i = np.empty(n, np.int32)
     i2s = np.full(index_space or n, -1, np.int32)
-    load().orc_reorder(ptr(np.ascontiguousarray(idx, np.uint32)), ptr(np.ascontiguousarray(in_rays, np.float32)),
+    _call(load().orc_reorder, ptr(np.ascontiguousarray(idx, np.uint32)), ptr(np.ascontiguousarray(in_rays, np.float32)),
                        ptr(out), ptr(np.ascontiguousarray(in_s2i, np.int32)), ptr(s2i), ptr(i2s), C.c_uint32(n))
     return out, s2i, i2s
 
 
 def sobol2d(i):
     x, y = C.c_float(), C.c_float()
-    load().orc_sobol2d(C.c_uint32(i), C.byref(x), C.byref(y))
+    _call(load().orc_sobol2d, C.c_uint32(i), C.byref(x), C.byref(y))
     return x.value, y.value
 
 
 def sincos_2pi(r):
     s, c = C.c_float(), C.c_float()
-    load().orc_sincos_2pi(C.c_float(r), C.byref(s), C.byref(c))
+    _call(load().orc_sincos_2pi, C.c_float(r), C.byref(s), C.byref(c))
     return s.value, c.value
 
 
@@ -131,7 +147,7 @@ def raygen_shadow(seeds, in_rays, in_res, light, radius, bb, bs, S):
     out = np.empty((ns, 8), np.float32)
     s2i = np.empty(ns, np.int32)
     i2s = np.empty(ns, np.int32)
-    load().orc_raygen_shadow(ptr(np.ascontiguousarray(seeds, np.uint32)), ptr(np.ascontiguousarray(in_rays, np.float32)),
+    _call(load().orc_raygen_shadow, ptr(np.ascontiguousarray(seeds, np.uint32)), ptr(np.ascontiguousarray(in_rays, np.float32)),
                              ptr(np.ascontiguousarray(in_res, np.int32)), ptr(out), ptr(s2i), ptr(i2s),
                              ptr(_f(light, 3)), C.c_float(radius), C.c_int(bb), C.c_int(bs), C.c_int(S))
     return out, s2i, i2s
@@ -152,7 +168,7 @@ def raygen_path(seeds, geom: HostGeometry, in_rays, in_i2p, in_res, decreases, a
     dec = np.ascontiguousarray(decreases, np.float32).copy()
     out = np.zeros((n, 8), np.float32)
     out_i2p = np.zeros(n, np.int32)
-    cnt = load().orc_raygen_path(ptr(seeds), ptr(geom.table), ptr(np.ascontiguousarray(in_rays, np.float32)),
+    cnt = _call(load().orc_raygen_path, ptr(seeds), ptr(geom.table), ptr(np.ascontiguousarray(in_rays, np.float32)),
                                  ptr(out), ptr(np.ascontiguousarray(in_i2p, np.int32)), ptr(out_i2p),
                                  ptr(np.ascontiguousarray(in_res, np.int32)), ptr(dec), C.c_uint32(n),
                                  C.c_float(albedo))
@@ -162,7 +178,7 @@ def raygen_path(seeds, geom: HostGeometry, in_rays, in_i2p, in_res, decreases, a
 def reconstruct_smooth(rays, res, i2p, pixels, decreases, geom: HostGeometry, light, bg, spp):
     px = np.ascontiguousarray(pixels, np.float32).copy()
     n = rays.shape[0]
-    load().orc_reconstruct_smooth(ptr(np.ascontiguousarray(rays, np.float32)), ptr(np.ascontiguousarray(res, np.int32)),
+    _call(load().orc_reconstruct_smooth, ptr(np.ascontiguousarray(rays, np.float32)), ptr(np.ascontiguousarray(res, np.int32)),
                                   ptr(np.ascontiguousarray(i2p, np.int32)), ptr(px),
                                   ptr(np.ascontiguousarray(decreases, np.float32)), ptr(geom.table), ptr(_f(light, 3)),
                                   ptr(_f(bg, 3)), C.c_uint32(n), C.c_int(spp))
@@ -171,7 +187,7 @@ def reconstruct_smooth(rays, res, i2p, pixels, decreases, geom: HostGeometry, li
 
 def reconstruct_shadow(res, i2p, i2s, in_pixels, out_pixels, bb, bs, S, replace=False):
     out = np.ascontiguousarray(out_pixels, np.float32).copy()
-    load().orc_reconstruct_shadow(ptr(np.ascontiguousarray(res, np.int32)), ptr(np.ascontiguousarray(i2p, np.int32)),
+    _call(load().orc_reconstruct_shadow, ptr(np.ascontiguousarray(res, np.int32)), ptr(np.ascontiguousarray(i2p, np.int32)),
                                   ptr(np.ascontiguousarray(i2s, np.int32)),
                                   ptr(np.ascontiguousarray(in_pixels, np.float32)), ptr(out), C.c_int(bb),
                                   C.c_int(bs), C.c_int(S), C.c_int(1 if replace else 0))
@@ -180,13 +196,13 @@ def reconstruct_shadow(res, i2p, i2s, in_pixels, out_pixels, bb, bs, S, replace=
 
 def count_hits(res):
     res = np.ascontiguousarray(res, np.int32)
-    return int(load().orc_count_hits(ptr(res), C.c_uint32(res.shape[0])))
+    return int(_call(load().orc_count_hits, ptr(res), C.c_uint32(res.shape[0])))
 
 
 def interpolate_colors(frame_pixels, pixels, frame_index, key, white):
     fp = np.ascontiguousarray(frame_pixels, np.float32).copy()
     pp = np.ascontiguousarray(pixels, np.float32).copy()
-    load().orc_interpolate_colors(ptr(fp), ptr(pp), C.c_uint32(fp.shape[0]), C.c_int(frame_index), C.c_float(key),
+    _call(load().orc_interpolate_colors, ptr(fp), ptr(pp), C.c_uint32(fp.shape[0]), C.c_int(frame_index), C.c_float(key),
                                   C.c_float(white))
     return fp, pp
 
@@ -196,7 +212,7 @@ def trace_bvh2(nodes: np.ndarray, tris: np.ndarray, rays, closest=True, ray_inde
     n = rays.shape[0]
     res = np.empty((n, 4), np.int32)
     ri = None if ray_index is None else np.ascontiguousarray(ray_index, np.uint32)
-    load().orc_trace_bvh2(ptr(nodes), ptr(tris), ptr(rays), ptr(res), ptr(ri), C.c_uint32(n),
+    _call(load().orc_trace_bvh2, ptr(nodes), ptr(tris), ptr(rays), ptr(res), ptr(ri), C.c_uint32(n),
                           C.c_int(1 if closest else 0))
     return res
 
@@ -208,7 +224,7 @@ class Fp64Scene:
         self._pos = np.ascontiguousarray(positions, np.float32)
         self._idx = np.ascontiguousarray(indices, np.uint32)
         gf = None if geometry_first is None else np.ascontiguousarray(geometry_first, np.uint32)
-        self.h = load().orc_fp64_scene_create(ptr(self._pos), ptr(self._idx), C.c_uint32(self._idx.shape[0]),
+        self.h = _call(load().orc_fp64_scene_create, ptr(self._pos), ptr(self._idx), C.c_uint32(self._idx.shape[0]),
                                               ptr(gf), C.c_uint32(0 if gf is None else gf.shape[0]))
 
     def trace(self, rays, closest=True):
@@ -216,13 +232,13 @@ class Fp64Scene:
         n = rays.shape[0]
         t = np.empty(n, np.float64)
         tri = np.empty(n, np.int64)
-        load().orc_fp64_trace(C.c_void_p(self.h), ptr(rays), C.c_uint32(n), C.c_int(1 if closest else 0), ptr(t),
+        _call(load().orc_fp64_trace, C.c_void_p(self.h), ptr(rays), C.c_uint32(n), C.c_int(1 if closest else 0), ptr(t),
                               ptr(tri))
         return t, tri
 
     def __del__(self):
         try:
-            load().orc_fp64_scene_destroy(C.c_void_p(self.h))
+            _call(load().orc_fp64_scene_destroy, C.c_void_p(self.h))
         except Exception:
             pass
 
@@ -233,7 +249,7 @@ def render_frame(nodes, tris, geom: HostGeometry, smin, smax, light, bg, s2w, ey
     px = np.zeros((n, 4), np.float32) if pixels is None else np.ascontiguousarray(pixels, np.float32).copy()
     fp = np.zeros((n, 4), np.float32)
     st = Stats()
-    load().orc_render_frame(ptr(nodes), ptr(tris), ptr(geom.table), ptr(_f(smin, 3)), ptr(_f(smax, 3)),
+    _call(load().orc_render_frame, ptr(nodes), ptr(tris), ptr(geom.table), ptr(_f(smin, 3)), ptr(_f(smax, 3)),
                             ptr(_f(light, 3)), ptr(_f(bg, 3)), ptr(_f(s2w, 16)), ptr(_f(eye, 3)), C.c_float(zfar),
                             C.c_int(w), C.c_int(h), C.byref(cfg), ptr(px), ptr(fp), C.byref(st))
     return px, fp, st

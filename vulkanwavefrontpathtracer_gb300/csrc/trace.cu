@@ -34,7 +34,7 @@ struct RayT {
     float tmin;
     int kx, ky, kz;
     float sx, sy, sz;
-    uint32_t oct;  // bit k set when d[k] < 0
+    uint32_t oct;  // bit k = sign bit of d[k]
 };
 
 __device__ __forceinline__ float comp(const f3& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
@@ -68,7 +68,10 @@ __device__ __forceinline__ RayT setup_ray(const float4& r0, const float4& r1) {
     r.sx = __fdiv_rn(comp(r.d, kx), dz);
     r.sy = __fdiv_rn(comp(r.d, ky), dz);
     r.sz = __fdiv_rn(1.0f, dz);
-    r.oct = (r.d.x < 0.0f ? 1u : 0u) | (r.d.y < 0.0f ? 2u : 0u) | (r.d.z < 0.0f ? 4u : 0u);
+    // Sign bits (not d < 0): -0.0 has a negative reciprocal in safe_inv, and
+    // the BVH8 near/far plane choice must agree with the sign of inv.
+    r.oct = (__float_as_uint(r.d.x) >> 31) | ((__float_as_uint(r.d.y) >> 31) << 1) |
+            ((__float_as_uint(r.d.z) >> 31) << 2);
     return r;
 }
 
@@ -233,6 +236,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
 // --------------------------------------------------------- BVH8 (chosen)
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xFFu; }
 
+// Byte b of w as an exact float: the byte is permuted into the mantissa of
+// 2^23 (bits 0x4B000000), then 2^23 is subtracted -- one PRMT and one FADD
+// instead of an integer-to-float conversion.
+__device__ __forceinline__ float q2f(uint32_t w, int b) {
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b)), 8388608.0f);
+}
+
 template <bool CLOSEST>
 __global__ void __launch_bounds__(kBlock) k_trace_bvh8(const float4* __restrict__ nodes,
                                                        const float4* __restrict__ tris,
@@ -286,31 +296,37 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh8(const float4* __restrict_
         float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
         float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
         float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
-        uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
-        uint32_t qlx[2] = {__float_as_uint(n2.x), __float_as_uint(n2.y)};
-        uint32_t qly[2] = {__float_as_uint(n2.z), __float_as_uint(n2.w)};
-        uint32_t qlz[2] = {__float_as_uint(n3.x), __float_as_uint(n3.y)};
-        uint32_t qhx[2] = {__float_as_uint(n3.z), __float_as_uint(n3.w)};
-        uint32_t qhy[2] = {__float_as_uint(n4.x), __float_as_uint(n4.y)};
-        uint32_t qhz[2] = {__float_as_uint(n4.z), __float_as_uint(n4.w)};
+        // Near/far planes per axis chosen once per node by the ray octant
+        // (d < 0: the hi plane is entered first).
+        const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
+        uint32_t nx[2] = {sx ? __float_as_uint(n3.z) : __float_as_uint(n2.x), sx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
+        uint32_t fx[2] = {sx ? __float_as_uint(n2.x) : __float_as_uint(n3.z), sx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
+        uint32_t ny[2] = {sy ? __float_as_uint(n4.x) : __float_as_uint(n2.z), sy ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
+        uint32_t fy[2] = {sy ? __float_as_uint(n2.z) : __float_as_uint(n4.x), sy ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
+        uint32_t nz[2] = {sz ? __float_as_uint(n4.z) : __float_as_uint(n3.x), sz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
+        uint32_t fz[2] = {sz ? __float_as_uint(n3.x) : __float_as_uint(n4.z), sz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
+        // Meta bytes, four at a time: inner children (bits 4 and 3 set) get
+        // their hit bit permuted by the octant; child_bits is the unary count.
+        uint32_t bit_index[2], child_bits[2];
+        const uint32_t oct4 = oct * 0x01010101u;
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            uint32_t m4 = __float_as_uint(w ? n1.w : n1.z);
+            uint32_t inner4 = (m4 & (m4 << 1)) & 0x10101010u;
+            uint32_t perm = oct4 & ((inner4 >> 4) * 7u);
+            bit_index[w] = (m4 ^ perm) & 0x1F1F1F1Fu;
+            child_bits[w] = (m4 >> 5) & 0x07070707u;
+        }
         uint32_t hitmask = 0;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            int w = c >> 2, b = c & 3;
-            uint32_t meta = byte_of(w ? meta_hi : meta_lo, b);
-            float x0 = __fmaf_rn((float)byte_of(qlx[w], b), ax, bx);
-            float x1 = __fmaf_rn((float)byte_of(qhx[w], b), ax, bx);
-            float y0 = __fmaf_rn((float)byte_of(qly[w], b), ay, by);
-            float y1 = __fmaf_rn((float)byte_of(qhy[w], b), ay, by);
-            float z0 = __fmaf_rn((float)byte_of(qlz[w], b), az, bz);
-            float z1 = __fmaf_rn((float)byte_of(qhz[w], b), az, bz);
-            float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), r.tmin));
-            float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
-            if (meta != 0u && tn <= tf * kBoxSlack) {
-                uint32_t inner = (imask >> c) & 1u;
-                uint32_t pos = (meta & 31u) ^ (inner ? oct : 0u);
-                hitmask |= (meta >> 5) << pos;
-            }
+            const int w = c >> 2, b = c & 3;
+            float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
+            float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
+            float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
+            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+            float tf = fminf(fminf(tfx, tfy), fminf(tfz, h.t));
+            if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
         }
         uint32_t tri_base = __float_as_uint(n1.y);
         ng = make_uint2(__float_as_uint(n1.x), (hitmask & 0xFF000000u) | imask);
