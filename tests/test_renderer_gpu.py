@@ -56,8 +56,25 @@ def run_pair(wf, orc, dev, small, w, h, frames=1, **opts):
     return N(px), N(fp), st, o_px, o_fp, o_st
 
 
-def same_bits(a, b):
-    return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+class same_bits:
+    """Truthy when the two float arrays are bit-identical; its repr reports
+    how many pixels differ, by how much, and the first few."""
+
+    def __init__(self, a, b):
+        a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+        self.ok = np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        bad = np.nonzero((a.view(np.uint32) != b.view(np.uint32)).any(axis=1))[0]
+        self.msg = "identical"
+        if bad.size:
+            d = np.abs(a[bad] - b[bad]).max()
+            first = ", ".join(f"{i}: {a[i]} vs {b[i]}" for i in bad[:3])
+            self.msg = f"{bad.size} of {len(a)} pixels differ (max abs diff {d:.3g}); {first}"
+
+    def __bool__(self):
+        return bool(self.ok)
+
+    def __repr__(self):
+        return self.msg
 
 
 @pytest.mark.parametrize("opts", [

@@ -47,8 +47,13 @@ constexpr int tile_of() {
     return kSortBlock * SortCfg<K>::kKpt;
 }
 
-__device__ __forceinline__ uint32_t digit_of(uint32_t k, int shift) { return (k >> shift) & 0xFFu; }
-__device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift) { return (uint32_t)(k >> shift) & 0xFFu; }
+// Digit mask of pass p: the top pass keeps only the bits below key_bits.
+__host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p) {
+    int bits = key_bits - 8 * p;
+    return bits >= 8 ? 0xFFu : ((1u << bits) - 1u);
+}
+__device__ __forceinline__ uint32_t digit_of(uint32_t k, int shift, uint32_t dmask) { return (k >> shift) & dmask; }
+__device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift, uint32_t dmask) { return (uint32_t)(k >> shift) & dmask; }
 
 // Exclusive scan of one value per thread over a 256-thread block.
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp) {
@@ -73,14 +78,14 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 template <typename K>
 __global__ void __launch_bounds__(kSortBlock) k_sort_hist(const K* __restrict__ keys, uint32_t n,
                                                            const uint32_t* __restrict__ n_dev, int passes,
-                                                           uint32_t* __restrict__ hist) {
+                                                           int key_bits, uint32_t* __restrict__ hist) {
     __shared__ uint32_t s_h[8 * kRadix];
     for (int i = threadIdx.x; i < passes * kRadix; i += kSortBlock) s_h[i] = 0;
     __syncthreads();
     uint32_t count = load_count(n, n_dev);
     for (uint32_t i = blockIdx.x * kSortBlock + threadIdx.x; i < count; i += gridDim.x * kSortBlock) {
         K k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p * kRadix + digit_of(k, 8 * p)], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p * kRadix + digit_of(k, 8 * p, pass_mask(key_bits, p))], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * kRadix; i += kSortBlock) {
@@ -95,7 +100,7 @@ template <typename K>
 __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                          uint32_t n, const uint32_t* __restrict__ n_dev, int shift,
+                                                          uint32_t n, const uint32_t* __restrict__ n_dev, int shift, uint32_t dmask,
                                                           const uint32_t* __restrict__ hist,
                                                           uint32_t* __restrict__ lookback,
                                                           uint32_t* __restrict__ ticket) {
@@ -137,7 +142,7 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         bool ok = (base + k * 32) < count;
-        uint32_t d = digit_of(key[k], shift);
+        uint32_t d = digit_of(key[k], shift, dmask);
         uint32_t peers = __ballot_sync(0xffffffffu, ok);
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         if ((base + k * 32) < count) {
-            uint32_t dk = digit_of(key[k], shift);
+            uint32_t dk = digit_of(key[k], shift, dmask);
             uint32_t pos = s_loc[dk] + my_hist[dk] + rank[k];
             s_keys[pos] = key[k];
             s_vals[pos] = val[k];
@@ -211,7 +216,7 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
     const uint32_t tile_count = min((uint32_t)TILE, count - tile * TILE);
     for (uint32_t j = threadIdx.x; j < tile_count; j += kSortBlock) {
         K kk = s_keys[j];
-        uint32_t g = s_base[digit_of(kk, shift)] + j;
+        uint32_t g = s_base[digit_of(kk, shift, dmask)] + j;
         if (g < count) {  // only fails after a look-back timeout
             keys_out[g] = kk;
             vals_out[g] = s_vals[j];
@@ -277,7 +282,7 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
 
     unsigned hgrid = (unsigned)std::min<size_t>(((size_t)n + kSortBlock * 8 - 1) / (kSortBlock * 8), 152 * 4);
     if (hgrid == 0) hgrid = 1;
-    k_sort_hist<K><<<hgrid, kSortBlock, 0, s>>>(keys, n, n_dev, L.passes, hist);
+    k_sort_hist<K><<<hgrid, kSortBlock, 0, s>>>(keys, n, n_dev, L.passes, key_bits, hist);
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -296,7 +301,7 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     uint32_t* dst_v = alt_vals;
     unsigned grid = (unsigned)(L.tiles == 0 ? 1 : L.tiles);
     for (int p = 0; p < L.passes; ++p) {
-        k_onesweep<K><<<grid, kSortBlock, smem, s>>>(src_k, src_v, dst_k, dst_v, n, n_dev, 8 * p,
+        k_onesweep<K><<<grid, kSortBlock, smem, s>>>(src_k, src_v, dst_k, dst_v, n, n_dev, 8 * p, pass_mask(key_bits, p),
                                                      hist + p * kRadix, lookback + (size_t)p * L.tiles * kRadix,
                                                      tickets + p);
         count_launch();
