@@ -43,7 +43,7 @@ struct wfpt_scene {
     wfpt::HostBvh2 bvh2;  // plain-form BVH kept on the host for export
     wfpt::HostBvh8 bvh8;
     wfpt::SceneDevice dev;
-    void* bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     wfpt_scene_info info{};
     bool has2 = false, has8 = false, host_only = false;
 };
@@ -321,6 +321,11 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
         if (e == cudaSuccess && sc->has8 && !sc->host_only) {
             e = upload(&sc->bufs[2], b8.nodes.data(), b8.nodes.size() * sizeof(wfpt::Bvh8Node));
             if (e == cudaSuccess) e = upload(&sc->bufs[3], b8.tris.data(), b8.tris.size() * sizeof(wfpt::TriRec));
+        }
+        if (e == cudaSuccess && !sc->host_only) {
+            e = cudaMalloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+            if (e == cudaSuccess) e = cudaMemset(sc->bufs[4], 0, wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+            sc->dev.work = reinterpret_cast<uint32_t*>(sc->bufs[4]);
         }
         if (e != cudaSuccess) {
             wfpt_scene_destroy(sc);

@@ -76,11 +76,16 @@ void build_bvh2(const BuildInput& in, int max_leaf, HostBvh2& out);
 // Greedy collapse of a BVH2 (leaves <= 3 triangles) into the 8-wide format.
 void build_bvh8(const HostBvh2& bvh2, HostBvh8& out);
 
+// Persistent-traversal work counters: kWorkSlots slots of 16 u32 each
+// (next ray, warps finished), zeroed at scene creation.
+constexpr int kWorkSlots = 64;
+
 struct SceneDevice {
     const float4* bvh2_nodes = nullptr;
     const float4* bvh2_tris = nullptr;
     const float4* bvh8_nodes = nullptr;
     const float4* bvh8_tris = nullptr;
+    uint32_t* work = nullptr;
 };
 
 }  // namespace wfpt

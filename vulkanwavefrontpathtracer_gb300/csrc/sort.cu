@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_hist(const K* __restrict__ 
 // One digit pass.  Dynamic shared memory: TILE keys, TILE values,
 // kSortWarps*256 per-warp digit counters, 256 global bases, 256 local offsets.
 template <typename K>
-__global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ keys_in,
+__global__ void __launch_bounds__(kSortBlock, 4) k_onesweep(const K* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                           uint32_t n, const uint32_t* __restrict__ n_dev, int shift, uint32_t dmask,
@@ -128,14 +128,11 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
     const uint32_t base = tile * TILE + warp * 32 * KPT + lane;
 
     K key[KPT];
-    uint32_t val[KPT];
     uint32_t rank[KPT];
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         uint32_t i = base + k * 32;
-        bool ok = i < count;
-        key[k] = ok ? keys_in[i] : (K)0;
-        val[k] = ok ? vals_in[i] : 0u;
+        key[k] = i < count ? keys_in[i] : (K)0;
     }
     uint32_t* my_hist = s_hist + warp * kRadix;
     // Warp-level stable ranking: keys are visited in input order (k, lane).
@@ -178,22 +175,37 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
     } else {
         atomicExch(lb, kLbAggregate | run);
         excl = 0;
+        // Walk back over predecessors, reading kChunk of them with
+        // independent loads per round trip; stop at the first inclusive
+        // prefix, wait (bounded) on an entry that is not published yet.
+        constexpr int kChunk = 8;
         int32_t j = (int32_t)tile - 1;
         uint32_t spins = 0;
-        while (j >= 0) {
-            uint32_t st = *((volatile uint32_t*)(lookback + (size_t)j * kRadix + d));
-            uint32_t flag = st & ~kLbValue;
-            if (flag == 0u) {
+        bool done = false;
+        while (!done && j >= 0) {
+            uint32_t st[kChunk];
+#pragma unroll
+            for (int q = 0; q < kChunk; ++q)
+                st[q] = (j - q >= 0) ? *((volatile uint32_t*)(lookback + (size_t)(j - q) * kRadix + d))
+                                     : uint32_t(kLbPrefix);
+            int used = 0;
+#pragma unroll
+            for (int q = 0; q < kChunk; ++q) {
+                if (done || used < q) continue;  // stopped earlier in this chunk
+                uint32_t flag = st[q] & ~kLbValue;
+                if (flag == 0u) continue;  // not published: re-read from here
+                excl += st[q] & kLbValue;
+                used = q + 1;
+                if (flag == kLbPrefix) done = true;
+            }
+            j -= used;
+            if (!done && used < kChunk && j >= 0) {
                 if (++spins > kSpinLimit) {
                     raise_status(kErrTimeout);
                     break;
                 }
                 __nanosleep(32);
-                continue;
             }
-            excl += st & kLbValue;
-            if (flag == kLbPrefix) break;
-            --j;
         }
         atomicExch(lb, kLbPrefix | (excl + run));
     }
@@ -202,14 +214,16 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep(const K* __restrict__ k
     s_base[d] = excl - loc;
     __syncthreads();
 
-    // Stage the tile in digit order.
+    // Stage the tile in digit order; values are read here, straight from
+    // global memory into their sorted slot.
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
-        if ((base + k * 32) < count) {
+        uint32_t i = base + k * 32;
+        if (i < count) {
             uint32_t dk = digit_of(key[k], shift, dmask);
             uint32_t pos = s_loc[dk] + my_hist[dk] + rank[k];
             s_keys[pos] = key[k];
-            s_vals[pos] = val[k];
+            s_vals[pos] = vals_in[i];
         }
     }
     __syncthreads();

@@ -2,16 +2,21 @@
 // on a GPU without RT cores.
 //
 // Plain form  (WFPT_BVH2_FP32): binary BVH, each 64-byte node holds both
-//   children's FP32 boxes; while-while traversal with a per-thread stack.
+//   children's FP32 boxes; one thread per ray, while-while traversal with a
+//   per-thread stack.
 // Chosen form (WFPT_BVH8_Q8):   8-wide BVH, 80-byte nodes with an FP32
 //   origin, per-axis power-of-two scales and 8-bit child boxes rounded
 //   outward; children visited in ray-octant order, node groups on the stack
 //   (Ylitie, Karras, Laine: "Efficient Incoherent Ray Traversal on GPUs
-//   Through Compressed Wide BVHs", HPG 2017).
+//   Through Compressed Wide BVHs", HPG 2017).  Persistent warps: a lane
+//   whose ray is done takes the next ray from a global counter (one atomic
+//   per warp for all idle lanes), so warps stay full on incoherent rays.
 // Both use the watertight ray/triangle test of Woop, Benthin and Wald
 // (JCGT 2013), evaluated without FMA contraction, and the same closest-hit
 // rule (smallest t, ties to the smaller global triangle index), so both
 // forms return identical hits.
+#include <atomic>
+
 #include "common.cuh"
 #include "scene.h"
 #include "stages.cuh"
@@ -25,10 +30,10 @@ constexpr int kStack2 = 64;
 constexpr int kStack8 = 32;
 // Relative slack on box exit distances (about 2*gamma(3) for FP32).
 constexpr float kBoxSlack = 1.0000004f;
+constexpr uint32_t kNoRay = 0xFFFFFFFFu;
 
 struct RayT {
     f3 o;
-    f3 d;
     f3 inv;
     f3 oinv;  // o * inv
     float tmin;
@@ -48,15 +53,15 @@ __device__ __forceinline__ float safe_inv(float d) {
 __device__ __forceinline__ RayT setup_ray(const float4& r0, const float4& r1) {
     RayT r;
     r.o = mk(r0.x, r0.y, r0.z);
-    r.d = mk(r1.x, r1.y, r1.z);
+    f3 d = mk(r1.x, r1.y, r1.z);
     r.tmin = r0.w;
-    r.inv = mk(safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z));
+    r.inv = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
     r.oinv = mul(r.o, r.inv);
-    float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
     int kx = kz + 1 == 3 ? 0 : kz + 1;
     int ky = kx + 1 == 3 ? 0 : kx + 1;
-    if (comp(r.d, kz) < 0.0f) {
+    if (comp(d, kz) < 0.0f) {
         int t = kx;
         kx = ky;
         ky = t;
@@ -64,30 +69,32 @@ __device__ __forceinline__ RayT setup_ray(const float4& r0, const float4& r1) {
     r.kx = kx;
     r.ky = ky;
     r.kz = kz;
-    float dz = comp(r.d, kz);
-    r.sx = __fdiv_rn(comp(r.d, kx), dz);
-    r.sy = __fdiv_rn(comp(r.d, ky), dz);
+    float dz = comp(d, kz);
+    r.sx = __fdiv_rn(comp(d, kx), dz);
+    r.sy = __fdiv_rn(comp(d, ky), dz);
     r.sz = __fdiv_rn(1.0f, dz);
     // Sign bits (not d < 0): -0.0 has a negative reciprocal in safe_inv, and
     // the BVH8 near/far plane choice must agree with the sign of inv.
-    r.oct = (__float_as_uint(r.d.x) >> 31) | ((__float_as_uint(r.d.y) >> 31) << 1) |
-            ((__float_as_uint(r.d.z) >> 31) << 2);
+    r.oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
+            ((__float_as_uint(d.z) >> 31) << 2);
     return r;
 }
 
-struct Hit {
+// Closest-hit state: distance, tie-break key (global triangle index) and
+// the triangle record index; barycentrics are recomputed once at the end.
+struct HitS {
     float t;
-    uint32_t key;  // global triangle index of the current best hit
-    int prim, geom;
-    float u, v;
+    uint32_t key;
+    uint32_t rec;
 };
 
-// Watertight test; on acceptance updates `h` and returns true.
-__device__ __forceinline__ bool intersect_tri(const RayT& r, const float4* __restrict__ tris, uint32_t ti,
-                                              Hit& h) {
-    float4 a4 = __ldg(&tris[3 * ti + 0]);
-    float4 b4 = __ldg(&tris[3 * ti + 1]);
-    float4 c4 = __ldg(&tris[3 * ti + 2]);
+struct Uvw {
+    float U, V, W, det, T;
+    bool edge_ok;
+};
+
+// Woop-Benthin-Wald edge functions and scaled distance for one triangle.
+__device__ __forceinline__ Uvw tri_uvw(const RayT& r, const float4& a4, const float4& b4, const float4& c4) {
     f3 A = sub(mk(a4.x, a4.y, a4.z), r.o);
     f3 B = sub(mk(b4.x, b4.y, b4.z), r.o);
     f3 C = sub(mk(c4.x, c4.y, c4.z), r.o);
@@ -98,43 +105,62 @@ __device__ __forceinline__ bool intersect_tri(const RayT& r, const float4* __res
     float By = __fsub_rn(comp(B, r.ky), __fmul_rn(r.sy, Bkz));
     float Cx = __fsub_rn(comp(C, r.kx), __fmul_rn(r.sx, Ckz));
     float Cy = __fsub_rn(comp(C, r.ky), __fmul_rn(r.sy, Ckz));
-    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    Uvw o;
+    o.U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    o.V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    o.W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (o.U == 0.0f || o.V == 0.0f || o.W == 0.0f) {
         double cxby = (double)Cx * (double)By, cybx = (double)Cy * (double)Bx;
-        U = (float)(cxby - cybx);
+        o.U = (float)(cxby - cybx);
         double axcy = (double)Ax * (double)Cy, aycx = (double)Ay * (double)Cx;
-        V = (float)(axcy - aycx);
+        o.V = (float)(axcy - aycx);
         double bxay = (double)Bx * (double)Ay, byax = (double)By * (double)Ax;
-        W = (float)(bxay - byax);
+        o.W = (float)(bxay - byax);
     }
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-    float det = __fadd_rn(__fadd_rn(U, V), W);
-    if (det == 0.0f) return false;
+    o.edge_ok = !((o.U < 0.0f || o.V < 0.0f || o.W < 0.0f) && (o.U > 0.0f || o.V > 0.0f || o.W > 0.0f));
+    o.det = __fadd_rn(__fadd_rn(o.U, o.V), o.W);
     float Az = __fmul_rn(r.sz, Akz), Bz = __fmul_rn(r.sz, Bkz), Cz = __fmul_rn(r.sz, Ckz);
-    float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
-    float t = __fdiv_rn(T, det);
+    o.T = __fadd_rn(__fadd_rn(__fmul_rn(o.U, Az), __fmul_rn(o.V, Bz)), __fmul_rn(o.W, Cz));
+    return o;
+}
+
+// Watertight test of record `rec`; on acceptance updates `h`.
+__device__ __forceinline__ bool intersect_tri(const RayT& r, const float4* __restrict__ tris, uint32_t rec,
+                                              HitS& h) {
+    float4 a4 = __ldg(&tris[3 * rec + 0]);
+    float4 b4 = __ldg(&tris[3 * rec + 1]);
+    float4 c4 = __ldg(&tris[3 * rec + 2]);
+    Uvw q = tri_uvw(r, a4, b4, c4);
+    if (!q.edge_ok || q.det == 0.0f) return false;
+    float t = __fdiv_rn(q.T, q.det);
     if (!(t >= r.tmin)) return false;
     uint32_t key = __float_as_uint(c4.w);
     if (!(t < h.t || (t == h.t && key < h.key))) return false;
     h.t = t;
     h.key = key;
-    h.prim = __float_as_int(a4.w);
-    h.geom = __float_as_int(b4.w);
-    h.u = __fdiv_rn(V, det);
-    h.v = __fdiv_rn(W, det);
+    h.rec = rec;
     return true;
 }
 
-__device__ __forceinline__ void write_hit(int4* __restrict__ results, uint32_t ri, const Hit& h, bool found) {
+// Writes the RayResult of a finished ray (trace.comp:66-84).
+__device__ __forceinline__ void write_hit(int4* __restrict__ results, uint32_t ri, const RayT& r,
+                                          const float4* __restrict__ tris, const HitS& h, bool found) {
     int4 out;
     if (found) {
-        out = make_int4(h.prim, h.geom, __float_as_int(h.t), (int)pack_unorm2x16(h.u, h.v));
+        float4 a4 = __ldg(&tris[3 * h.rec + 0]);
+        float4 b4 = __ldg(&tris[3 * h.rec + 1]);
+        float4 c4 = __ldg(&tris[3 * h.rec + 2]);
+        Uvw q = tri_uvw(r, a4, b4, c4);  // same inputs, same edge functions as at acceptance
+        float u = __fdiv_rn(q.V, q.det), v = __fdiv_rn(q.W, q.det);
+        out = make_int4(__float_as_int(a4.w), __float_as_int(b4.w), __float_as_int(h.t), (int)pack_unorm2x16(u, v));
     } else {
         out = make_int4(-1, -1, __float_as_int(-1.0f), 0);
     }
     results[ri] = out;
+}
+
+__device__ __forceinline__ void write_miss(int4* __restrict__ results, uint32_t ri) {
+    results[ri] = make_int4(-1, -1, __float_as_int(-1.0f), 0);
 }
 
 // ------------------------------------------------------------ BVH2 (plain)
@@ -160,15 +186,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
     uint32_t ri = ray_index ? ray_index[i] : i;
     float4 r0 = rays[2 * ri + 0];
     float4 r1 = rays[2 * ri + 1];
-    Hit h;
-    h.t = r1.w;
-    h.key = 0xFFFFFFFFu;
-    bool found = false;
     if (!(r1.w >= r0.w)) {  // tmax < tmin (or NaN): empty interval
-        write_hit(results, ri, h, false);
+        write_miss(results, ri);
         return;
     }
     RayT r = setup_ray(r0, r1);
+    HitS h{r1.w, 0xFFFFFFFFu, 0u};
+    bool found = false;
     int stack[kStack2];
     int sp = 0;
     int node = 0;
@@ -230,7 +254,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
             node = stack[--sp];
         }
     }
-    write_hit(results, ri, h, found);
+    write_hit(results, ri, r, tris, h, found);
 }
 
 // --------------------------------------------------------- BVH8 (chosen)
@@ -243,35 +267,122 @@ __device__ __forceinline__ float q2f(uint32_t w, int b) {
     return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b)), 8388608.0f);
 }
 
-template <bool CLOSEST>
-__global__ void __launch_bounds__(kBlock) k_trace_bvh8(const float4* __restrict__ nodes,
-                                                       const float4* __restrict__ tris,
-                                                       const float4* __restrict__ rays, int4* __restrict__ results,
-                                                       const uint32_t* __restrict__ ray_index, uint32_t n,
-                                                       const uint32_t* __restrict__ n_dev) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= load_count(n, n_dev)) return;
-    uint32_t ri = ray_index ? ray_index[i] : i;
-    float4 r0 = rays[2 * ri + 0];
-    float4 r1 = rays[2 * ri + 1];
-    Hit h;
-    h.t = r1.w;
-    h.key = 0xFFFFFFFFu;
-    bool found = false;
-    if (!(r1.w >= r0.w)) {
-        write_hit(results, ri, h, false);
-        return;
-    }
-    RayT r = setup_ray(r0, r1);
+// Intersects the eight children of a BVH8 node.  Returns the hit mask:
+// bits 24..31 inner children (octant-permuted slot order, highest first),
+// bits 0..23 triangles relative to *tri_base; *child_base and *imask out.
+__device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ nd, const RayT& r, float tcur,
+                                                    uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
+    float4 n0 = __ldg(nd + 0);
+    float4 n1 = __ldg(nd + 1);
+    float4 n2 = __ldg(nd + 2);
+    float4 n3 = __ldg(nd + 3);
+    float4 n4 = __ldg(nd + 4);
     const uint32_t oct = r.oct;
+    uint32_t ew = __float_as_uint(n0.w);
+    float scx = __uint_as_float((ew & 0xFFu) << 23);
+    float scy = __uint_as_float(((ew >> 8) & 0xFFu) << 23);
+    float scz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
+    imask = ew >> 24;
+    child_base = __float_as_uint(n1.x);
+    tri_base = __float_as_uint(n1.y);
+    // Slab distance = q * (scale*inv) + (p - o) * inv.
+    float ax = __fmul_rn(scx, r.inv.x), ay = __fmul_rn(scy, r.inv.y), az = __fmul_rn(scz, r.inv.z);
+    float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
+    float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
+    float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
+    // Near/far planes per axis chosen once per node by the ray octant
+    // (d < 0: the hi plane is entered first).
+    const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
+    uint32_t nx[2] = {sx ? __float_as_uint(n3.z) : __float_as_uint(n2.x), sx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
+    uint32_t fx[2] = {sx ? __float_as_uint(n2.x) : __float_as_uint(n3.z), sx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
+    uint32_t ny[2] = {sy ? __float_as_uint(n4.x) : __float_as_uint(n2.z), sy ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
+    uint32_t fy[2] = {sy ? __float_as_uint(n2.z) : __float_as_uint(n4.x), sy ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
+    uint32_t nz[2] = {sz ? __float_as_uint(n4.z) : __float_as_uint(n3.x), sz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
+    uint32_t fz[2] = {sz ? __float_as_uint(n3.x) : __float_as_uint(n4.z), sz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
+    // Meta bytes, four at a time: inner children (bits 4 and 3 set) get
+    // their hit bit permuted by the octant; child_bits is the unary count.
+    uint32_t bit_index[2], child_bits[2];
+    const uint32_t oct4 = oct * 0x01010101u;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+        uint32_t m4 = __float_as_uint(w ? n1.w : n1.z);
+        uint32_t inner4 = (m4 & (m4 << 1)) & 0x10101010u;
+        uint32_t perm = oct4 & ((inner4 >> 4) * 7u);
+        bit_index[w] = (m4 ^ perm) & 0x1F1F1F1Fu;
+        child_bits[w] = (m4 >> 5) & 0x07070707u;
+    }
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int w = c >> 2, b = c & 3;
+        float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
+        float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
+        float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
+        float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+        float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur));
+        if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
+    }
+    return hitmask;
+}
+
+// Persistent-warp traversal.  work[0] = next ray to hand out, work[1] =
+// warps finished; the last warp to finish resets both, so the counters
+// need no reset between launches that use them one after another.
+template <bool CLOSEST>
+__global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restrict__ nodes,
+                                                          const float4* __restrict__ tris,
+                                                          const float4* __restrict__ rays, int4* __restrict__ results,
+                                                          const uint32_t* __restrict__ ray_index, uint32_t n,
+                                                          const uint32_t* __restrict__ n_dev,
+                                                          uint32_t* __restrict__ work, uint32_t refill) {
+    const uint32_t count = load_count(n, n_dev);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     uint2 stack[kStack8];
     int sp = 0;
-    // Node group: x = child base index, y = node hit bits (24..31) | imask (0..7).
-    uint2 ng = make_uint2(0u, 0x80000000u);
+    uint32_t ri = kNoRay;
+    bool exhausted = false, found = false;
+    RayT r;
+    HitS h;
+    uint2 ng = make_uint2(0u, 0u);  // node group: child base, hit bits 24..31 | imask 0..7
     for (;;) {
+        // Refill idle lanes with new rays (one atomic per warp).
+        bool want = ri == kNoRay && !exhausted;
+        uint32_t want_mask = __ballot_sync(0xffffffffu, want);
+        uint32_t busy_mask = __ballot_sync(0xffffffffu, ri != kNoRay);
+        if (want_mask != 0u && (__popc(want_mask) >= refill || busy_mask == 0u)) {
+            uint32_t leader = __ffs(want_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&work[0], __popc(want_mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (want) {
+                uint32_t i = base + __popc(want_mask & lt_mask);
+                if (i < count) {
+                    uint32_t idx = ray_index ? ray_index[i] : i;
+                    float4 r0 = rays[2 * idx + 0];
+                    float4 r1 = rays[2 * idx + 1];
+                    if (!(r1.w >= r0.w)) {  // empty interval: miss, lane stays idle
+                        write_miss(results, idx);
+                    } else {
+                        ri = idx;
+                        r = setup_ray(r0, r1);
+                        h = HitS{r1.w, 0xFFFFFFFFu, 0u};
+                        found = false;
+                        sp = 0;
+                        ng = make_uint2(0u, 0x80000000u);  // root as the only child of a virtual group
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ri != kNoRay || !exhausted) == 0u) break;
+        if (ri == kNoRay) continue;
+
+        // One node: pick the nearest child of the current group.
         uint32_t bit = 31u - __clz(ng.y);
         ng.y &= ~(1u << bit);
-        uint32_t slot = (bit - 24u) ^ oct;
+        uint32_t slot = (bit - 24u) ^ r.oct;
         uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
         if (ng.y > 0x00FFFFFFu) {
             if (sp < kStack8) {
@@ -280,77 +391,54 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh8(const float4* __restrict_
                 raise_status(kErrBounds);
             }
         }
-        const float4* nd = nodes + 5 * (size_t)node;
-        float4 n0 = __ldg(nd + 0);
-        float4 n1 = __ldg(nd + 1);
-        float4 n2 = __ldg(nd + 2);
-        float4 n3 = __ldg(nd + 3);
-        float4 n4 = __ldg(nd + 4);
-        uint32_t ew = __float_as_uint(n0.w);
-        float scx = __uint_as_float((ew & 0xFFu) << 23);
-        float scy = __uint_as_float(((ew >> 8) & 0xFFu) << 23);
-        float scz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
-        uint32_t imask = ew >> 24;
-        // Slab distance = q * (scale*inv) + (p - o) * inv.
-        float ax = __fmul_rn(scx, r.inv.x), ay = __fmul_rn(scy, r.inv.y), az = __fmul_rn(scz, r.inv.z);
-        float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
-        float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
-        float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
-        // Near/far planes per axis chosen once per node by the ray octant
-        // (d < 0: the hi plane is entered first).
-        const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
-        uint32_t nx[2] = {sx ? __float_as_uint(n3.z) : __float_as_uint(n2.x), sx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
-        uint32_t fx[2] = {sx ? __float_as_uint(n2.x) : __float_as_uint(n3.z), sx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
-        uint32_t ny[2] = {sy ? __float_as_uint(n4.x) : __float_as_uint(n2.z), sy ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
-        uint32_t fy[2] = {sy ? __float_as_uint(n2.z) : __float_as_uint(n4.x), sy ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
-        uint32_t nz[2] = {sz ? __float_as_uint(n4.z) : __float_as_uint(n3.x), sz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
-        uint32_t fz[2] = {sz ? __float_as_uint(n3.x) : __float_as_uint(n4.z), sz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
-        // Meta bytes, four at a time: inner children (bits 4 and 3 set) get
-        // their hit bit permuted by the octant; child_bits is the unary count.
-        uint32_t bit_index[2], child_bits[2];
-        const uint32_t oct4 = oct * 0x01010101u;
-#pragma unroll
-        for (int w = 0; w < 2; ++w) {
-            uint32_t m4 = __float_as_uint(w ? n1.w : n1.z);
-            uint32_t inner4 = (m4 & (m4 << 1)) & 0x10101010u;
-            uint32_t perm = oct4 & ((inner4 >> 4) * 7u);
-            bit_index[w] = (m4 ^ perm) & 0x1F1F1F1Fu;
-            child_bits[w] = (m4 >> 5) & 0x07070707u;
-        }
-        uint32_t hitmask = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int w = c >> 2, b = c & 3;
-            float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
-            float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
-            float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
-            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-            float tf = fminf(fminf(tfx, tfy), fminf(tfz, h.t));
-            if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
-        }
-        uint32_t tri_base = __float_as_uint(n1.y);
-        ng = make_uint2(__float_as_uint(n1.x), (hitmask & 0xFF000000u) | imask);
+        uint32_t child_base, tri_base, imask;
+        uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, h.t, child_base, tri_base, imask);
+        ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
         uint32_t tg = hitmask & 0x00FFFFFFu;
-        bool stop = false;
+        bool finished = false;
         while (tg != 0u) {
             uint32_t tb = __ffs(tg) - 1u;
             tg &= tg - 1u;
             if (intersect_tri(r, tris, tri_base + tb, h)) {
                 found = true;
                 if (!CLOSEST) {
-                    stop = true;
+                    finished = true;
                     break;
                 }
             }
         }
-        if (stop) break;
-        if (ng.y <= 0x00FFFFFFu) {
-            if (sp == 0) break;
-            ng = stack[--sp];
+        if (!finished && ng.y <= 0x00FFFFFFu) {
+            if (sp == 0) {
+                finished = true;
+            } else {
+                ng = stack[--sp];
+            }
+        }
+        if (finished) {
+            write_hit(results, ri, r, tris, h, found);
+            ri = kNoRay;
         }
     }
-    write_hit(results, ri, h, found);
+    // Last warp out resets the work counters for the next launch.
+    if (lane == 0) {
+        uint32_t warps = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&work[1], 1u) == warps - 1u) {
+            work[0] = 0u;
+            work[1] = 0u;
+            __threadfence();
+        }
+    }
 }
+
+// Work-counter slots (16 u32 apart) handed out round robin, so concurrent
+// traces on different streams do not share a counter.
+static std::atomic<uint32_t> g_slot{0};
+static int g_blocks_per_sm[2] = {0, 0};
+static int g_num_sms = 0;
+static uint32_t g_refill = 8;
+
+void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
@@ -360,10 +448,23 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
     const float4* rr = reinterpret_cast<const float4*>(rays);
     int4* out = reinterpret_cast<int4*>(results);
     if (kind == WFPT_BVH8_Q8) {
+        if (g_num_sms == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false>, kBlock, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true>, kBlock, 0);
+        }
+        unsigned pgrid = (unsigned)(g_num_sms * (closest ? g_blocks_per_sm[1] : g_blocks_per_sm[0]));
+        if (pgrid == 0) pgrid = 1;
+        if (grid < pgrid) pgrid = grid;
+        uint32_t* work = sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
         if (closest)
-            k_trace_bvh8<true><<<grid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev);
+            k_trace_bvh8<true><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
+                                                       work, g_refill);
         else
-            k_trace_bvh8<false><<<grid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev);
+            k_trace_bvh8<false><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
+                                                        work, g_refill);
     } else {
         if (closest)
             k_trace_bvh2<true><<<grid, kBlock, 0, s>>>(sc.bvh2_nodes, sc.bvh2_tris, rr, out, ray_index, n, n_dev);

@@ -9,6 +9,10 @@
 
 namespace wfpt {
 
+// Persistent BVH8 traversal refills a warp when at least this many lanes
+// are idle (1..32; 32 = only when the whole warp is idle).
+void set_trace_refill(uint32_t refill);
+
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
                          cudaStream_t s);
