@@ -326,6 +326,66 @@ def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
     }
 
 
+def make_wavefronts(wf, api, dev, scene, geom, cam, w, h, light, shadow_samples=2):
+    """Bounce-1 path rays (unsorted, as compacted) and the shadow rays of the
+    primary hits, built with the stage kernels."""
+    import torch
+    n = w * h
+    i2p_np, _ = api.pixel_table(w, h)
+    i2p = torch.from_numpy(i2p_np).to(dev)
+    s2w = api.camera_screen_to_world(cam.position, cam.rotation_deg, cam.fov_deg, w / h, cam.znear, cam.zfar)
+    prim = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    api.raygen_primary(s2w, i2p, prim, list(cam.position), 0, w, h, cam.zfar)
+    hits = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    api.trace(scene, wf.BVH8_Q8, prim, hits)
+    seeds = torch.empty(n, dtype=torch.int32, device=dev)
+    api.init_seeds(seeds, 1)
+    srays = torch.empty((n * shadow_samples, 8), dtype=torch.float32, device=dev)
+    s2i = torch.empty(n * shadow_samples, dtype=torch.int32, device=dev)
+    i2s = torch.empty(n * shadow_samples, dtype=torch.int32, device=dev)
+    api.raygen_shadow(seeds, prim, hits, srays, s2i, i2s, light, 1.0, 0, n, shadow_samples)
+    dec = torch.ones((n, 4), dtype=torch.float32, device=dev)
+    path = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    p_i2p = torch.empty(n, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    api.raygen_path(seeds, geom.table, prim, path, i2p, p_i2p, hits, dec, cnt)
+    m = int(cnt.item())
+    return path[:m].contiguous(), srays
+
+
+def run_sweep(args):
+    """Autotuner searches on the courtyard wavefronts (prints one JSON line)."""
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import autotune
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    dev = torch.device("cuda", 0)
+    api = wf.api
+    W = COURTYARD
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx)
+    geom = api.Geometry(pos, nrm, idx, device=dev)
+    cam = api.make_camera(**W["camera"])
+    path, shadow = make_wavefronts(wf, api, dev, scene, geom, cam, args.width, args.height, W["light"])
+    keys = autotune.tune_keys(scene, path)
+    best = keys["best"]
+    if best["morton"] is not None and best["reorder"]:
+        # tune traversal on the reordered wavefront the renderer would trace
+        m = path.shape[0]
+        k = torch.empty(m, dtype=torch.int64, device=dev)
+        ids = torch.empty(m, dtype=torch.int32, device=dev)
+        api.morton(path, scene.bounds_min, scene.bounds_max - scene.bounds_min, best["morton"], k, ids)
+        api.sort_pairs(k, ids, best["key_bits"])
+        out = torch.empty_like(path)
+        api.reorder(ids, path, out, torch.arange(m, dtype=torch.int32, device=dev),
+                    torch.empty(m, dtype=torch.int32, device=dev), torch.empty(m, dtype=torch.int32, device=dev))
+        path = out
+    trav = autotune.tune_traversal(scene, path, shadow)
+    print(json.dumps({"keys": keys, "traversal": trav, "resolution": [args.width, args.height]}))
+
+
 def run_micro_only(args):
     import torch
 
@@ -421,7 +481,11 @@ def main():
                     help="only the bounce-1 microbenchmark (small profiling case with --width/--height)")
     ap.add_argument("--width", type=int, default=COURTYARD["width"])
     ap.add_argument("--height", type=int, default=COURTYARD["height"])
+    ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")
     args = ap.parse_args()
+    if args.sweep:
+        run_sweep(args)
+        return
     if args.micro_only:
         run_micro_only(args)
         return

@@ -117,6 +117,16 @@ wfpt_status wfpt_device_status(uint32_t* flags);
  * benchmarks; no counterpart in the reference). */
 uint64_t wfpt_kernel_launch_count(void);
 
+/* Process-wide tuning knobs (no counterpart in the reference; set by the
+ * autotuner).  Keys:
+ *   "trace.bvh8.refill"    refill a persistent warp when this many lanes
+ *                          are idle (1..32, default 8)
+ *   "trace.bvh8.postpone"  postpone a node's triangle tests while fewer than
+ *                          this many lanes have triangles (0..32, 0 = off)
+ * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */
+wfpt_status wfpt_tune_set(const char* key, int64_t value);
+wfpt_status wfpt_tune_get(const char* key, int64_t* value);
+
 /* ------------------------------------------------------ host-side helpers */
 
 /* PixelTable::recalculate (Ray/PixelTable.cpp:21-99): index<->pixel bijection

@@ -215,3 +215,19 @@ def test_cpu_frame_runs(wf, orc):
     assert st.primary == w * h
     assert 0 < st.path <= 3 * w * h
     assert np.all(np.isfinite(fp)) and np.all(fp[:, 3] == 1.0)
+
+
+def test_tuning_knobs(wf):
+    api = wf.api
+    old = api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone")
+    try:
+        api.tune_set("trace.bvh8.refill", 4)
+        api.tune_set("trace.bvh8.postpone", 6)
+        assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
+        for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
+                         ("no.such.knob", 1)):
+            with pytest.raises(wf.WfptError):
+                api.tune_set(key, bad)
+    finally:
+        api.tune_set("trace.bvh8.refill", old[0])
+        api.tune_set("trace.bvh8.postpone", old[1])

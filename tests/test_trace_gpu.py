@@ -144,3 +144,21 @@ def test_multi_geometry_ids(wf, dev):
     assert np.all((glob >= 0) & (glob < 3000))
     assert set(np.unique(hit[:, 1])) <= {0, 1, 2}
     assert np.all(hit[hit[:, 1] == 1, 0] < 1500) and np.all(hit[hit[:, 1] == 2, 0] < 500)
+
+
+@pytest.mark.parametrize("refill,postpone", [(1, 0), (32, 0), (8, 8), (4, 16)])
+def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone):
+    pos, idx, sc = soup
+    rays = random_rays(np.random.default_rng(12), 60000)
+    ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
+    ref_any = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=False)
+    old = wf.api.tune_get("trace.bvh8.refill"), wf.api.tune_get("trace.bvh8.postpone")
+    try:
+        wf.api.tune_set("trace.bvh8.refill", refill)
+        wf.api.tune_set("trace.bvh8.postpone", postpone)
+        assert np.array_equal(gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays), ref)
+        a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)
+        assert np.array_equal(a8[:, 0] >= 0, ref_any[:, 0] >= 0)
+    finally:
+        wf.api.tune_set("trace.bvh8.refill", old[0])
+        wf.api.tune_set("trace.bvh8.postpone", old[1])

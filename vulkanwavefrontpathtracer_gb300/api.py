@@ -51,6 +51,17 @@ def device_status() -> int:
     return flags.value
 
 
+def tune_set(key: str, value: int) -> None:
+    """Sets a process-wide tuning knob (see wfpt_tune_set in include/wfpt.h)."""
+    L.check(lib().wfpt_tune_set(key.encode(), int(value)))
+
+
+def tune_get(key: str) -> int:
+    v = C.c_int64(0)
+    L.check(lib().wfpt_tune_get(key.encode(), C.byref(v)))
+    return v.value
+
+
 # ------------------------------------------------------------ host helpers
 def pixel_table(width: int, height: int):
     i2p = np.empty(width * height, np.int32)

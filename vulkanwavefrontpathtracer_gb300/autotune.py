@@ -1,0 +1,104 @@
+"""Autotuner for the wavefront stages.
+
+Searches, on the GPU it runs on and for a given scene:
+  * the persistent BVH8 traversal knobs (warp refill threshold, triangle
+    postponing threshold), separately for closest-hit and any-hit rays;
+  * the Morton key layout (32-bit Aila, 48- and 64-bit 6-D) and whether to
+    reorder the rays, for a path-ray wavefront, by timing the composite
+    Morton + radix sort + reorder + trace.
+Timings use CUDA events over repeated launches on the current stream.  The
+result is a plain dict that `apply()` installs (traversal knobs are
+process-wide) and that a renderer configuration can take the key/reorder
+choice from.
+"""
+from __future__ import annotations
+
+import itertools
+from typing import Callable, Dict, Iterable
+
+from . import _lib as L
+from . import api
+
+
+def _timeit(fn: Callable[[], None], reps: int = 5, warm: int = 2) -> float:
+    import torch
+    stream = torch.cuda.current_stream()
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[int] = (1, 2, 4, 8, 16, 32),
+                   postpones: Iterable[int] = (0, 4, 8, 12), reps: int = 5) -> Dict:
+    """Grid search of (refill, postpone) for BVH8 closest-hit and any-hit
+    traversal; returns the best settings and the full table (ms)."""
+    import torch
+    dev = closest_rays.device
+    res_c = torch.empty((closest_rays.shape[0], 4), dtype=torch.int32, device=dev)
+    res_a = torch.empty((any_rays.shape[0], 4), dtype=torch.int32, device=dev)
+    old = (api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"))
+    table = []
+    try:
+        for refill, post in itertools.product(refills, postpones):
+            api.tune_set("trace.bvh8.refill", refill)
+            api.tune_set("trace.bvh8.postpone", post)
+            mc = _timeit(lambda: api.trace(scene, L.BVH8_Q8, closest_rays, res_c, closest_hit=True), reps)
+            ma = _timeit(lambda: api.trace(scene, L.BVH8_Q8, any_rays, res_a, closest_hit=False), reps)
+            table.append({"refill": refill, "postpone": post, "closest_ms": mc, "any_ms": ma})
+    finally:
+        api.tune_set("trace.bvh8.refill", old[0])
+        api.tune_set("trace.bvh8.postpone", old[1])
+    # The knobs are shared by both kinds of rays: weigh them by ray count.
+    nc, na = closest_rays.shape[0], any_rays.shape[0]
+    best = min(table, key=lambda e: e["closest_ms"] + e["any_ms"])
+    return {"refill": best["refill"], "postpone": best["postpone"], "table": table,
+            "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
+            "best_any_mrays_s": na / (best["any_ms"] * 1e-3) / 1e6}
+
+
+KEY_CHOICES = ((L.MORTON_AILA32, 32), (L.MORTON_6D48, 48), (L.MORTON_6D64, 63))
+
+
+def tune_keys(scene: api.Scene, path_rays, bvh_kind: int = L.BVH8_Q8, reps: int = 5) -> Dict:
+    """Times trace alone, and Morton + sort + (reorder | indirect) + trace for
+    each key layout; returns the fastest choice and the table (ms)."""
+    import torch
+    dev = path_rays.device
+    m = path_rays.shape[0]
+    res = torch.empty((m, 4), dtype=torch.int32, device=dev)
+    keys = torch.empty(m, dtype=torch.int64, device=dev)
+    ids = torch.empty(m, dtype=torch.int32, device=dev)
+    scratch = torch.empty(api.sort_scratch_bytes(m, 64), dtype=torch.uint8, device=dev)
+    s2i = torch.arange(m, dtype=torch.int32, device=dev)
+    out = torch.empty_like(path_rays)
+    os2i = torch.empty(m, dtype=torch.int32, device=dev)
+    oi2s = torch.empty(m, dtype=torch.int32, device=dev)
+    smin = scene.bounds_min
+    ssize = scene.bounds_max - scene.bounds_min
+    table = [{"morton": None, "reorder": False,
+              "ms": _timeit(lambda: api.trace(scene, bvh_kind, path_rays, res), reps)}]
+    for kind, bits in KEY_CHOICES:
+        for reorder in (False, True):
+            def step(kind=kind, bits=bits, reorder=reorder):
+                api.morton(path_rays, smin, ssize, kind, keys, ids)
+                api.sort_pairs(keys, ids, bits, scratch=scratch)
+                if reorder:
+                    api.reorder(ids, path_rays, out, s2i, os2i, oi2s)
+                    api.trace(scene, bvh_kind, out, res)
+                else:
+                    api.trace(scene, bvh_kind, path_rays, res, ray_index=ids)
+            table.append({"morton": kind, "key_bits": bits, "reorder": reorder, "ms": _timeit(step, reps)})
+    best = min(table, key=lambda e: e["ms"])
+    return {"best": best, "table": table}
+
+
+def apply(traversal: Dict) -> None:
+    api.tune_set("trace.bvh8.refill", traversal["refill"])
+    api.tune_set("trace.bvh8.postpone", traversal["postpone"])

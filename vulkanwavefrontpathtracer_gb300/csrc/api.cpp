@@ -83,6 +83,36 @@ const char* wfpt_last_error_message(void) { return g_last_error.c_str(); }
 
 uint64_t wfpt_kernel_launch_count(void) { return wfpt::launch_count(); }
 
+wfpt_status wfpt_tune_set(const char* key, int64_t value) {
+    if (!key) return invalid("null key");
+    std::string k(key);
+    if (k == "trace.bvh8.refill") {
+        if (value < 1 || value > 32) return invalid("trace.bvh8.refill must be in [1, 32]");
+        wfpt::set_trace_refill((uint32_t)value);
+        return WFPT_OK;
+    }
+    if (k == "trace.bvh8.postpone") {
+        if (value < 0 || value > 32) return invalid("trace.bvh8.postpone must be in [0, 32]");
+        wfpt::set_trace_postpone((uint32_t)value);
+        return WFPT_OK;
+    }
+    return invalid("unknown tuning key");
+}
+
+wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
+    if (!key || !value) return invalid("null argument");
+    std::string k(key);
+    if (k == "trace.bvh8.refill") {
+        *value = wfpt::get_trace_refill();
+        return WFPT_OK;
+    }
+    if (k == "trace.bvh8.postpone") {
+        *value = wfpt::get_trace_postpone();
+        return WFPT_OK;
+    }
+    return invalid("unknown tuning key");
+}
+
 wfpt_status wfpt_device_status(uint32_t* flags) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return from_cuda(e);

@@ -260,11 +260,12 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
 // --------------------------------------------------------- BVH8 (chosen)
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xFFu; }
 
-// Byte b of w as an exact float: the byte is permuted into the mantissa of
-// 2^23 (bits 0x4B000000), then 2^23 is subtracted -- one PRMT and one FADD
-// instead of an integer-to-float conversion.
-__device__ __forceinline__ float q2f(uint32_t w, int b) {
-    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b)), 8388608.0f);
+// 2^23 + (byte b of w), exactly, as a float: the byte is permuted into the
+// mantissa of 2^23 (bits 0x4B000000) -- one PRMT instead of an
+// integer-to-float conversion.  The 2^23 bias is folded into the slab
+// offset by the caller.
+__device__ __forceinline__ float q2f_biased(uint32_t w, int b) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b));
 }
 
 // Intersects the eight children of a BVH8 node.  Returns the hit mask:
@@ -285,11 +286,13 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
     imask = ew >> 24;
     child_base = __float_as_uint(n1.x);
     tri_base = __float_as_uint(n1.y);
-    // Slab distance = q * (scale*inv) + (p - o) * inv.
+    // Slab distance = q * (scale*inv) + (p - o) * inv, evaluated as
+    // (2^23 + q) * a + (b - 2^23 * a).  The rounding of the folded offset
+    // is at most half a grid step in t; child boxes carry a one-step margin.
     float ax = __fmul_rn(scx, r.inv.x), ay = __fmul_rn(scy, r.inv.y), az = __fmul_rn(scz, r.inv.z);
-    float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
-    float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
-    float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
+    float bx = __fmaf_rn(-8388608.0f, ax, __fmaf_rn(n0.x, r.inv.x, -r.oinv.x));
+    float by = __fmaf_rn(-8388608.0f, ay, __fmaf_rn(n0.y, r.inv.y, -r.oinv.y));
+    float bz = __fmaf_rn(-8388608.0f, az, __fmaf_rn(n0.z, r.inv.z, -r.oinv.z));
     // Near/far planes per axis chosen once per node by the ray octant
     // (d < 0: the hi plane is entered first).
     const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
@@ -315,9 +318,9 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int w = c >> 2, b = c & 3;
-        float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
-        float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
-        float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
+        float tnx = __fmaf_rn(q2f_biased(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f_biased(fx[w], b), ax, bx);
+        float tny = __fmaf_rn(q2f_biased(ny[w], b), ay, by), tfy = __fmaf_rn(q2f_biased(fy[w], b), ay, by);
+        float tnz = __fmaf_rn(q2f_biased(nz[w], b), az, bz), tfz = __fmaf_rn(q2f_biased(fz[w], b), az, bz);
         float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
         float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur));
         if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
                                                           const float4* __restrict__ rays, int4* __restrict__ results,
                                                           const uint32_t* __restrict__ ray_index, uint32_t n,
                                                           const uint32_t* __restrict__ n_dev,
-                                                          uint32_t* __restrict__ work, uint32_t refill) {
+                                                          uint32_t* __restrict__ work, uint32_t refill, uint32_t postpone) {
     const uint32_t count = load_count(n, n_dev);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -376,25 +379,44 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
                 }
             }
         }
+        const uint32_t busy = __ballot_sync(0xffffffffu, ri != kNoRay);
         if (__ballot_sync(0xffffffffu, ri != kNoRay || !exhausted) == 0u) break;
         if (ri == kNoRay) continue;
 
-        // One node: pick the nearest child of the current group.
-        uint32_t bit = 31u - __clz(ng.y);
-        ng.y &= ~(1u << bit);
-        uint32_t slot = (bit - 24u) ^ r.oct;
-        uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+        // The current group is either a node group (hit bits 24..31) or a
+        // triangle group popped from the stack (bits 0..23, base in x).
+        uint32_t tri_base = 0, tg = 0;
         if (ng.y > 0x00FFFFFFu) {
-            if (sp < kStack8) {
-                stack[sp++] = ng;
-            } else {
-                raise_status(kErrBounds);
+            // One node: pick the nearest child of the current group.
+            uint32_t bit = 31u - __clz(ng.y);
+            ng.y &= ~(1u << bit);
+            uint32_t slot = (bit - 24u) ^ r.oct;
+            uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+            if (ng.y > 0x00FFFFFFu) {
+                if (sp < kStack8) {
+                    stack[sp++] = ng;
+                } else {
+                    raise_status(kErrBounds);
+                }
+            }
+            uint32_t child_base, imask;
+            uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, h.t, child_base, tri_base, imask);
+            ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
+            tg = hitmask & 0x00FFFFFFu;
+        } else {
+            tri_base = ng.x;
+            tg = ng.y;
+            ng = make_uint2(0u, 0u);
+        }
+        // Postpone a node's triangles while few lanes of the warp have any
+        // and more nodes remain: they wait on the stack as a triangle group.
+        if (postpone != 0u) {
+            uint32_t with_tris = __ballot_sync(busy, tg != 0u);
+            if (tg != 0u && ng.y > 0x00FFFFFFu && (uint32_t)__popc(with_tris) < postpone && sp < kStack8) {
+                stack[sp++] = make_uint2(tri_base, tg);
+                tg = 0;
             }
         }
-        uint32_t child_base, tri_base, imask;
-        uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, h.t, child_base, tri_base, imask);
-        ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
-        uint32_t tg = hitmask & 0x00FFFFFFu;
         bool finished = false;
         while (tg != 0u) {
             uint32_t tb = __ffs(tg) - 1u;
@@ -439,6 +461,10 @@ static int g_num_sms = 0;
 static uint32_t g_refill = 8;
 
 void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
+static uint32_t g_postpone = 0;
+void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
+uint32_t get_trace_refill() { return g_refill; }
+uint32_t get_trace_postpone() { return g_postpone; }
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
@@ -461,10 +487,10 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
         uint32_t* work = sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
         if (closest)
             k_trace_bvh8<true><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
-                                                       work, g_refill);
+                                                       work, g_refill, g_postpone);
         else
             k_trace_bvh8<false><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
-                                                        work, g_refill);
+                                                        work, g_refill, g_postpone);
     } else {
         if (closest)
             k_trace_bvh2<true><<<grid, kBlock, 0, s>>>(sc.bvh2_nodes, sc.bvh2_tris, rr, out, ray_index, n, n_dev);

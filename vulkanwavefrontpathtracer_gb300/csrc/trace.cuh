@@ -12,6 +12,11 @@ namespace wfpt {
 // Persistent BVH8 traversal refills a warp when at least this many lanes
 // are idle (1..32; 32 = only when the whole warp is idle).
 void set_trace_refill(uint32_t refill);
+// Postpone a node's triangle tests while fewer than this many lanes of the
+// warp have triangles to test (0 = never).
+void set_trace_postpone(uint32_t lanes);
+uint32_t get_trace_refill();
+uint32_t get_trace_postpone();
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
