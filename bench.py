@@ -383,7 +383,10 @@ def run_sweep(args):
                     torch.empty(m, dtype=torch.int32, device=dev), torch.empty(m, dtype=torch.int32, device=dev))
         path = out
     trav = autotune.tune_traversal(scene, path, shadow)
-    print(json.dumps({"keys": keys, "traversal": trav, "resolution": [args.width, args.height]}))
+    work = {f"{form}_{kind}": autotune.measure_work(scene, rays, bvh, closest)
+            for form, bvh in (("bvh2", wf.BVH2_FP32), ("bvh8", wf.BVH8_Q8))
+            for kind, rays, closest in (("path", path, True), ("shadow", shadow, False))}
+    print(json.dumps({"keys": keys, "traversal": trav, "work": work, "resolution": [args.width, args.height]}))
 
 
 def run_micro_only(args):

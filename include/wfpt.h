@@ -123,9 +123,15 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          are idle (1..32, default 8)
  *   "trace.bvh8.postpone"  postpone a node's triangle tests while fewer than
  *                          this many lanes have triangles (0..32, 0 = off)
+ *   "trace.count"          1 = launch the counting traversal kernels, which
+ *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */
 wfpt_status wfpt_tune_set(const char* key, int64_t value);
 wfpt_status wfpt_tune_get(const char* key, int64_t* value);
+/* Counters of the counting traversal kernels (synchronises): out[0] node
+ * visits, out[1] triangle tests, out[2] rays, out[3] persistent-warp loop
+ * iterations; reset != 0 zeroes them. */
+wfpt_status wfpt_trace_counters(uint64_t out[4], int reset);
 
 /* ------------------------------------------------------ host-side helpers */
 

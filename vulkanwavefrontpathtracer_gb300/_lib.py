@@ -113,6 +113,7 @@ _SIGS = {
     "wfpt_kernel_launch_count": (c_u64, []),
     "wfpt_tune_set": (c_int, [C.c_char_p, C.c_int64]),
     "wfpt_tune_get": (c_int, [C.c_char_p, C.POINTER(C.c_int64)]),
+    "wfpt_trace_counters": (c_int, [C.POINTER(c_u64), c_int]),
     "wfpt_pixel_table": (c_int, [c_int, c_int, c_void_p, c_void_p]),
     "wfpt_camera_screen_to_world": (c_int, [P_f32, P_f32, c_float, c_float, c_float, c_float, P_f32]),
     "wfpt_init_seeds": (c_int, [c_void_p, c_u32, c_int, c_void_p]),

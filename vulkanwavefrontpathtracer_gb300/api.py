@@ -62,6 +62,14 @@ def tune_get(key: str) -> int:
     return v.value
 
 
+def trace_counters(reset: bool = True) -> dict:
+    """Counters of the counting traversal kernels (enable with
+    tune_set("trace.count", 1))."""
+    out = (C.c_uint64 * 4)()
+    L.check(lib().wfpt_trace_counters(out, 1 if reset else 0))
+    return {"nodes": out[0], "tris": out[1], "rays": out[2], "warp_iters": out[3]}
+
+
 # ------------------------------------------------------------ host helpers
 def pixel_table(width: int, height: int):
     i2p = np.empty(width * height, np.int32)

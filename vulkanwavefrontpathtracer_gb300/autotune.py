@@ -99,6 +99,27 @@ def tune_keys(scene: api.Scene, path_rays, bvh_kind: int = L.BVH8_Q8, reps: int 
     return {"best": best, "table": table}
 
 
+def measure_work(scene: api.Scene, rays, bvh_kind: int, closest: bool) -> Dict:
+    """Node visits and triangle tests per ray (counting kernel variants)."""
+    import torch
+    res = torch.empty((rays.shape[0], 4), dtype=torch.int32, device=rays.device)
+    old = api.tune_get("trace.count")
+    api.tune_set("trace.count", 1)
+    try:
+        api.trace_counters(reset=True)
+        api.trace(scene, bvh_kind, rays, res, closest_hit=closest)
+        c = api.trace_counters(reset=True)
+    finally:
+        api.tune_set("trace.count", old)
+    n = max(1, c["rays"])
+    out = {"rays": c["rays"], "nodes_per_ray": c["nodes"] / n, "tris_per_ray": c["tris"] / n}
+    if c["warp_iters"]:
+        # lanes busy per warp loop iteration: node steps / iterations
+        out["warp_iters"] = c["warp_iters"]
+        out["node_steps_per_iter"] = c["nodes"] / c["warp_iters"]
+    return out
+
+
 def apply(traversal: Dict) -> None:
     api.tune_set("trace.bvh8.refill", traversal["refill"])
     api.tune_set("trace.bvh8.postpone", traversal["postpone"])

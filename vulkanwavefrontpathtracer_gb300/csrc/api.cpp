@@ -96,7 +96,19 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_trace_postpone((uint32_t)value);
         return WFPT_OK;
     }
+    if (k == "trace.count") {
+        if (value < 0 || value > 1) return invalid("trace.count must be 0 or 1");
+        wfpt::set_trace_count(value != 0);
+        return WFPT_OK;
+    }
     return invalid("unknown tuning key");
+}
+
+wfpt_status wfpt_trace_counters(uint64_t out[4], int reset) {
+    if (!out) return invalid("null output");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = wfpt::trace_counters(out, reset != 0);
+    return from_cuda(e);
 }
 
 wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
@@ -108,6 +120,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "trace.bvh8.postpone") {
         *value = wfpt::get_trace_postpone();
+        return WFPT_OK;
+    }
+    if (k == "trace.count") {
+        *value = wfpt::get_trace_count() ? 1 : 0;
         return WFPT_OK;
     }
     return invalid("unknown tuning key");

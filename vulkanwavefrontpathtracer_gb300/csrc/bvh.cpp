@@ -390,26 +390,21 @@ struct Collapser {
         // Node box and quantisation grid.
         Box nb;
         for (auto& c : ch) nb.grow(c.box);
-        // The grid starts one step below the node box and spans 254 steps
-        // past it, so every child box fits in [1, 254] and can be widened by
-        // one step on each side: the traversal's slab arithmetic may be off by
-        // half a step (it folds the byte-to-float bias into the offset).
         float scale[3];
         for (int k = 0; k < 3; ++k) {
+            node.p[k] = nb.lo[k];
             float ext = nb.hi[k] - nb.lo[k];
             int ex = -126;
             if (ext > 0.0f) {
                 int e2;
-                std::frexp(ext / 252.0f, &e2);
+                std::frexp(ext / 255.0f, &e2);
                 ex = e2;
             }
             for (;;) {
                 ex = std::max(-126, std::min(127, ex));
                 scale[k] = std::ldexp(1.0f, ex);
-                node.p[k] = nb.lo[k] - scale[k];
-                bool lo_ok = node.p[k] + scale[k] <= nb.lo[k];
-                bool hi_ok = node.p[k] + 254.0f * scale[k] >= nb.hi[k];
-                if ((lo_ok && hi_ok) || ex == 127) break;
+                float top = node.p[k] + 255.0f * scale[k];
+                if (top >= nb.hi[k] || ex == 127) break;
                 ++ex;
             }
             node.e[k] = (uint8_t)(ex + 127);
@@ -462,8 +457,6 @@ struct Collapser {
                 int qh = (int)std::max(0.0f, std::min(255.0f, hi));
                 while (ql > 0 && node.p[k] + (float)ql * sc > c.box.lo[k]) --ql;
                 while (qh < 255 && node.p[k] + (float)qh * sc < c.box.hi[k]) ++qh;
-                ql = std::max(0, ql - 1);  // one-step margin (see the grid set-up above)
-                qh = std::min(255, qh + 1);
                 uint8_t* qlo = k == 0 ? node.qlo_x : (k == 1 ? node.qlo_y : node.qlo_z);
                 uint8_t* qhi = k == 0 ? node.qhi_x : (k == 1 ? node.qhi_y : node.qhi_z);
                 qlo[s] = (uint8_t)ql;

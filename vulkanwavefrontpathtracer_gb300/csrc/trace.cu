@@ -32,6 +32,17 @@ constexpr int kStack8 = 32;
 constexpr float kBoxSlack = 1.0000004f;
 constexpr uint32_t kNoRay = 0xFFFFFFFFu;
 
+// Work counters of the counting kernel variants: node visits, triangle
+// tests, rays, warp loop iterations (persistent kernel only).
+static __device__ unsigned long long g_counts[4];
+
+__device__ __forceinline__ void add_counts(uint32_t nodes, uint32_t tris, uint32_t rays, uint32_t iters) {
+    atomicAdd(&g_counts[0], (unsigned long long)nodes);
+    atomicAdd(&g_counts[1], (unsigned long long)tris);
+    atomicAdd(&g_counts[2], (unsigned long long)rays);
+    if (iters) atomicAdd(&g_counts[3], (unsigned long long)iters);
+}
+
 struct RayT {
     f3 o;
     f3 inv;
@@ -175,7 +186,7 @@ __device__ __forceinline__ void box2(const RayT& r, float lox, float hix, float 
     hit = tn <= tf * kBoxSlack;
 }
 
-template <bool CLOSEST>
+template <bool CLOSEST, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict__ nodes,
                                                        const float4* __restrict__ tris,
                                                        const float4* __restrict__ rays, int4* __restrict__ results,
@@ -193,6 +204,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
     RayT r = setup_ray(r0, r1);
     HitS h{r1.w, 0xFFFFFFFFu, 0u};
     bool found = false;
+    uint32_t c_nodes = 0, c_tris = 0;
     int stack[kStack2];
     int sp = 0;
     int node = 0;
@@ -200,6 +212,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
     while (!done) {
         // Inner nodes.
         while (node >= 0) {
+            if (COUNT) ++c_nodes;
             float4 a = __ldg(&nodes[4 * node + 0]);
             float4 b = __ldg(&nodes[4 * node + 1]);
             float4 c = __ldg(&nodes[4 * node + 2]);
@@ -238,6 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
             uint32_t code = ~(uint32_t)node;
             uint32_t first = code >> 3, cnt = (code & 7u) + 1u;
             for (uint32_t k = 0; k < cnt; ++k) {
+                if (COUNT) ++c_tris;
                 if (intersect_tri(r, tris, first + k, h)) {
                     found = true;
                     if (!CLOSEST) break;
@@ -255,17 +269,17 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
         }
     }
     write_hit(results, ri, r, tris, h, found);
+    if (COUNT) add_counts(c_nodes, c_tris, 1u, 0u);
 }
 
 // --------------------------------------------------------- BVH8 (chosen)
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xFFu; }
 
-// 2^23 + (byte b of w), exactly, as a float: the byte is permuted into the
-// mantissa of 2^23 (bits 0x4B000000) -- one PRMT instead of an
-// integer-to-float conversion.  The 2^23 bias is folded into the slab
-// offset by the caller.
-__device__ __forceinline__ float q2f_biased(uint32_t w, int b) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b));
+// Byte b of w as an exact float: the byte is permuted into the mantissa of
+// 2^23 (bits 0x4B000000), then 2^23 is subtracted -- one PRMT and one FADD
+// instead of an integer-to-float conversion.
+__device__ __forceinline__ float q2f(uint32_t w, int b) {
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b)), 8388608.0f);
 }
 
 // Intersects the eight children of a BVH8 node.  Returns the hit mask:
@@ -286,13 +300,11 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
     imask = ew >> 24;
     child_base = __float_as_uint(n1.x);
     tri_base = __float_as_uint(n1.y);
-    // Slab distance = q * (scale*inv) + (p - o) * inv, evaluated as
-    // (2^23 + q) * a + (b - 2^23 * a).  The rounding of the folded offset
-    // is at most half a grid step in t; child boxes carry a one-step margin.
+    // Slab distance = q * (scale*inv) + (p - o) * inv.
     float ax = __fmul_rn(scx, r.inv.x), ay = __fmul_rn(scy, r.inv.y), az = __fmul_rn(scz, r.inv.z);
-    float bx = __fmaf_rn(-8388608.0f, ax, __fmaf_rn(n0.x, r.inv.x, -r.oinv.x));
-    float by = __fmaf_rn(-8388608.0f, ay, __fmaf_rn(n0.y, r.inv.y, -r.oinv.y));
-    float bz = __fmaf_rn(-8388608.0f, az, __fmaf_rn(n0.z, r.inv.z, -r.oinv.z));
+    float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
+    float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
+    float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
     // Near/far planes per axis chosen once per node by the ray octant
     // (d < 0: the hi plane is entered first).
     const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
@@ -318,9 +330,9 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int w = c >> 2, b = c & 3;
-        float tnx = __fmaf_rn(q2f_biased(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f_biased(fx[w], b), ax, bx);
-        float tny = __fmaf_rn(q2f_biased(ny[w], b), ay, by), tfy = __fmaf_rn(q2f_biased(fy[w], b), ay, by);
-        float tnz = __fmaf_rn(q2f_biased(nz[w], b), az, bz), tfz = __fmaf_rn(q2f_biased(fz[w], b), az, bz);
+        float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
+        float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
+        float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
         float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
         float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur));
         if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
@@ -331,7 +343,7 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
 // Persistent-warp traversal.  work[0] = next ray to hand out, work[1] =
 // warps finished; the last warp to finish resets both, so the counters
 // need no reset between launches that use them one after another.
-template <bool CLOSEST>
+template <bool CLOSEST, bool COUNT>
 __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restrict__ nodes,
                                                           const float4* __restrict__ tris,
                                                           const float4* __restrict__ rays, int4* __restrict__ results,
@@ -348,6 +360,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
     RayT r;
     HitS h;
     uint2 ng = make_uint2(0u, 0u);  // node group: child base, hit bits 24..31 | imask 0..7
+    uint32_t c_nodes = 0, c_tris = 0, c_rays = 0, c_iters = 0;
     for (;;) {
         // Refill idle lanes with new rays (one atomic per warp).
         bool want = ri == kNoRay && !exhausted;
@@ -381,6 +394,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
         }
         const uint32_t busy = __ballot_sync(0xffffffffu, ri != kNoRay);
         if (__ballot_sync(0xffffffffu, ri != kNoRay || !exhausted) == 0u) break;
+        if (COUNT && lane == 0) ++c_iters;
         if (ri == kNoRay) continue;
 
         // The current group is either a node group (hit bits 24..31) or a
@@ -400,6 +414,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
                 }
             }
             uint32_t child_base, imask;
+            if (COUNT) ++c_nodes;
             uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, h.t, child_base, tri_base, imask);
             ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
             tg = hitmask & 0x00FFFFFFu;
@@ -421,6 +436,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
         while (tg != 0u) {
             uint32_t tb = __ffs(tg) - 1u;
             tg &= tg - 1u;
+            if (COUNT) ++c_tris;
             if (intersect_tri(r, tris, tri_base + tb, h)) {
                 found = true;
                 if (!CLOSEST) {
@@ -439,8 +455,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
         if (finished) {
             write_hit(results, ri, r, tris, h, found);
             ri = kNoRay;
+            if (COUNT) ++c_rays;
         }
     }
+    if (COUNT) add_counts(c_nodes, c_tris, c_rays, c_iters);
     // Last warp out resets the work counters for the next launch.
     if (lane == 0) {
         uint32_t warps = gridDim.x * (blockDim.x / 32);
@@ -464,6 +482,21 @@ void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 3
 static uint32_t g_postpone = 0;
 void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
 uint32_t get_trace_refill() { return g_refill; }
+static bool g_count = false;
+void set_trace_count(bool on) { g_count = on; }
+bool get_trace_count() { return g_count; }
+
+cudaError_t trace_counters(uint64_t out[4], bool reset) {
+    unsigned long long v[4];
+    cudaError_t e = cudaMemcpyFromSymbol(v, g_counts, sizeof(v));
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < 4; ++i) out[i] = v[i];
+    if (reset) {
+        unsigned long long z[4] = {0, 0, 0, 0};
+        e = cudaMemcpyToSymbol(g_counts, z, sizeof(z));
+    }
+    return e;
+}
 uint32_t get_trace_postpone() { return g_postpone; }
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
@@ -478,24 +511,21 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             int dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false>, kBlock, 0);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true>, kBlock, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false, false>, kBlock, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true, false>, kBlock, 0);
         }
         unsigned pgrid = (unsigned)(g_num_sms * (closest ? g_blocks_per_sm[1] : g_blocks_per_sm[0]));
         if (pgrid == 0) pgrid = 1;
         if (grid < pgrid) pgrid = grid;
         uint32_t* work = sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
-        if (closest)
-            k_trace_bvh8<true><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
-                                                       work, g_refill, g_postpone);
-        else
-            k_trace_bvh8<false><<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev,
-                                                        work, g_refill, g_postpone);
+        auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
+                          : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);
+        k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, work, g_refill,
+                                    g_postpone);
     } else {
-        if (closest)
-            k_trace_bvh2<true><<<grid, kBlock, 0, s>>>(sc.bvh2_nodes, sc.bvh2_tris, rr, out, ray_index, n, n_dev);
-        else
-            k_trace_bvh2<false><<<grid, kBlock, 0, s>>>(sc.bvh2_nodes, sc.bvh2_tris, rr, out, ray_index, n, n_dev);
+        auto k2 = closest ? (g_count ? k_trace_bvh2<true, true> : k_trace_bvh2<true, false>)
+                          : (g_count ? k_trace_bvh2<false, true> : k_trace_bvh2<false, false>);
+        k2<<<grid, kBlock, 0, s>>>(sc.bvh2_nodes, sc.bvh2_tris, rr, out, ray_index, n, n_dev);
     }
     count_launch();
     return cudaGetLastError();

@@ -17,6 +17,11 @@ void set_trace_refill(uint32_t refill);
 void set_trace_postpone(uint32_t lanes);
 uint32_t get_trace_refill();
 uint32_t get_trace_postpone();
+// Counting variants of the traversal kernels (node visits, triangle tests,
+// rays, persistent-warp iterations) for diagnostics.
+void set_trace_count(bool on);
+bool get_trace_count();
+cudaError_t trace_counters(uint64_t out[4], bool reset);
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
