@@ -91,6 +91,20 @@ __device__ __forceinline__ f3 faceforward(f3 n, f3 i, f3 nref) {
 
 __device__ __forceinline__ f3 ld_origin(const float4& a) { return {a.x, a.y, a.z}; }
 
+// Three-input minimum / maximum (one instruction on sm_100 and later);
+// same NaN handling as fminf/fmaxf, and exact, so
+// max3(a, b, c) == fmaxf(fmaxf(a, b), c) bit for bit.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // GLSL packUnorm2x16 / unpackUnorm2x16.
 __device__ __forceinline__ uint32_t pack_unorm2x16(float u, float v) {
     float cu = fminf(fmaxf(u, 0.0f), 1.0f);

@@ -180,8 +180,8 @@ __device__ __forceinline__ void box2(const RayT& r, float lox, float hix, float 
     float x0 = __fmaf_rn(lox, r.inv.x, -r.oinv.x), x1 = __fmaf_rn(hix, r.inv.x, -r.oinv.x);
     float y0 = __fmaf_rn(loy, r.inv.y, -r.oinv.y), y1 = __fmaf_rn(hiy, r.inv.y, -r.oinv.y);
     float z0 = __fmaf_rn(loz, r.inv.z, -r.oinv.z), z1 = __fmaf_rn(hiz, r.inv.z, -r.oinv.z);
-    float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), r.tmin));
-    float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tcur));
+    float tn = fmaxf(max3f(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)), r.tmin);
+    float tf = fminf(min3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)), tcur);
     tnear = tn;
     hit = tn <= tf * kBoxSlack;
 }
@@ -326,16 +326,26 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
         bit_index[w] = (m4 ^ perm) & 0x1F1F1F1Fu;
         child_bits[w] = (m4 >> 5) & 0x07070707u;
     }
-    uint32_t hitmask = 0;
+    // Box tests: bit c of `hit8` is set when child c's box is hit.
+    uint32_t hit8 = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int w = c >> 2, b = c & 3;
         float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
         float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
         float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
-        float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-        float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur));
-        if (tn <= tf * kBoxSlack) hitmask |= byte_of(child_bits[w], b) << byte_of(bit_index[w], b);
+        float tn = fmaxf(max3f(tnx, tny, tnz), r.tmin);
+        float tf = fminf(min3f(tfx, tfy, tfz), tcur);
+        if (tn <= tf * kBoxSlack) hit8 |= 1u << c;
+    }
+    // Hit bits of the hit children only (empty slots have child_bits 0).
+    uint32_t hitmask = 0;
+    while (hit8) {
+        int c = __ffs(hit8) - 1;
+        hit8 &= hit8 - 1u;
+        uint32_t bits = (c < 4 ? child_bits[0] : child_bits[1]) >> (8 * (c & 3));
+        uint32_t idx = (c < 4 ? bit_index[0] : bit_index[1]) >> (8 * (c & 3));
+        hitmask |= (bits & 0xFFu) << (idx & 0xFFu);
     }
     return hitmask;
 }
@@ -356,17 +366,26 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
     uint2 stack[kStack8];
     int sp = 0;
     uint32_t ri = kNoRay;
+    // Lane state: idle (no ray), tracing, or done (result held in registers
+    // until the next refill of the warp writes it, so the divergent write-out
+    // runs once per refill instead of once per finished ray).
+    enum : uint32_t { kIdle = 0, kTracing = 1, kDone = 2 };
+    uint32_t state = kIdle;
     bool exhausted = false, found = false;
     RayT r;
     HitS h;
     uint2 ng = make_uint2(0u, 0u);  // node group: child base, hit bits 24..31 | imask 0..7
     uint32_t c_nodes = 0, c_tris = 0, c_rays = 0, c_iters = 0;
     for (;;) {
-        // Refill idle lanes with new rays (one atomic per warp).
-        bool want = ri == kNoRay && !exhausted;
+        // Refill non-tracing lanes with new rays (one atomic per warp).
+        bool want = state != kTracing && !exhausted;
         uint32_t want_mask = __ballot_sync(0xffffffffu, want);
-        uint32_t busy_mask = __ballot_sync(0xffffffffu, ri != kNoRay);
+        uint32_t busy_mask = __ballot_sync(0xffffffffu, state == kTracing);
         if (want_mask != 0u && (__popc(want_mask) >= refill || busy_mask == 0u)) {
+            if (state == kDone) {
+                write_hit(results, ri, r, tris, h, found);
+                state = kIdle;
+            }
             uint32_t leader = __ffs(want_mask) - 1u;
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(&work[0], __popc(want_mask));
@@ -381,6 +400,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
                         write_miss(results, idx);
                     } else {
                         ri = idx;
+                        state = kTracing;
                         r = setup_ray(r0, r1);
                         h = HitS{r1.w, 0xFFFFFFFFu, 0u};
                         found = false;
@@ -392,10 +412,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
                 }
             }
         }
-        const uint32_t busy = __ballot_sync(0xffffffffu, ri != kNoRay);
-        if (__ballot_sync(0xffffffffu, ri != kNoRay || !exhausted) == 0u) break;
+        const uint32_t busy = __ballot_sync(0xffffffffu, state == kTracing);
+        if (__ballot_sync(0xffffffffu, state != kIdle || !exhausted) == 0u) break;
         if (COUNT && lane == 0) ++c_iters;
-        if (ri == kNoRay) continue;
+        if (state != kTracing) continue;
 
         // The current group is either a node group (hit bits 24..31) or a
         // triangle group popped from the stack (bits 0..23, base in x).
@@ -453,8 +473,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
             }
         }
         if (finished) {
-            write_hit(results, ri, r, tris, h, found);
-            ri = kNoRay;
+            state = kDone;
             if (COUNT) ++c_rays;
         }
     }
