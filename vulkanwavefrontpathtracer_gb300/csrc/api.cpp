@@ -350,7 +350,7 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
         }
         wfpt::HostBvh8& b8 = sc->bvh8;
         if (bvh_kinds_mask & (1 << WFPT_BVH8_Q8)) {
-            wfpt::build_bvh2(in, 3, for8);
+            wfpt::build_bvh2(in, 1, for8);  // single-triangle leaves: the collapse decides leaf sizes
             wfpt::build_bvh8(for8, b8);
             sc->has8 = true;
             if (!sc->has2) sc->bvh2 = for8;

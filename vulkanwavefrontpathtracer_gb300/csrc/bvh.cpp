@@ -356,12 +356,16 @@ struct Collapser {
             if (b.empty()) continue;
             ch.push_back({b, n.link[k], false});
         }
-        for (auto& c : ch) c.leaf = c.link < 0 || count_link(c.link) <= 3;
+        // Greedy fill: split the child of largest surface area while slots
+        // remain, small subtrees included (a split gives tighter boxes).  Only
+        // when the node is full (or nothing can be split) do subtrees of at
+        // most three triangles become leaf children; larger ones become inner
+        // children.  BVH2 leaves (link < 0) cannot be split.
         while (ch.size() < 8) {
             int best = -1;
             float best_area = -1.0f;
             for (int i = 0; i < (int)ch.size(); ++i) {
-                if (ch[i].leaf) continue;
+                if (ch[i].link < 0) continue;
                 float a = ch[i].box.area();
                 if (a > best_area) {
                     best_area = a;
@@ -374,13 +378,12 @@ struct Collapser {
             for (int k = 0; k < 2; ++k) {
                 Box b = child_box(m, k);
                 if (b.empty()) continue;
-                Child c{b, m.link[k], false};
-                c.leaf = c.link < 0 || count_link(c.link) <= 3;
-                repl.push_back(c);
+                repl.push_back(Child{b, m.link[k], false});
             }
             ch.erase(ch.begin() + best);  // at most 6 left, so the two children fit
             ch.insert(ch.end(), repl.begin(), repl.end());
         }
+        for (auto& c : ch) c.leaf = c.link < 0 || count_link(c.link) <= 3;
         Bvh8Node node;
         std::memset(&node, 0, sizeof(node));
         if (ch.empty()) {  // empty scene: a root without children
