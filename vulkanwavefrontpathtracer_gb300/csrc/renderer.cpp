@@ -107,12 +107,83 @@ struct wfpt_renderer {
     bool stats_pending = false;
     float frame_ms = 0.0f;
 
+    // Frame graph: captured once per (configuration, resolution, buffers,
+    // stream); replayed with the per-frame values in fp_dev.
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    wfpt::FrameParams* fp_dev = nullptr;
+    uint64_t graph_kernels = 0;  // kernels per replay (for the launch count)
+    struct GraphKey {
+        wfpt_renderer_config cfg;
+        int w, h;
+        const void *pixels, *frame_pixels, *stream, *scene, *geoms;
+        float light[3], bg[3], smin[3], smax[3];
+    } graph_key{};
+    bool graph_valid = false;
+
+    GraphKey make_key(float* pixels, float* frame_pixels, cudaStream_t s) const {
+        GraphKey k;
+        std::memset(&k, 0, sizeof(k));
+        k.cfg = cfg;
+        k.w = width;
+        k.h = height;
+        k.pixels = pixels;
+        k.frame_pixels = frame_pixels;
+        k.stream = s;
+        k.scene = scene;
+        k.geoms = geoms;
+        for (int i = 0; i < 3; ++i) {
+            k.light[i] = light[i];
+            k.bg[i] = bg[i];
+            k.smin[i] = smin[i];
+            k.smax[i] = smax[i];
+        }
+        return k;
+    }
+
+    // Renders through the frame graph, capturing it first when needed.
+    cudaError_t render_graph(const float* s2w, const float* eye, float zfar, float* pixels, float* frame_pixels,
+                             cudaStream_t s) {
+        cudaError_t e;
+        if (!fp_dev && (e = cudaMalloc(&fp_dev, sizeof(wfpt::FrameParams))) != cudaSuccess) return e;
+        if ((e = wfpt::sort_prepare()) != cudaSuccess) return e;
+        if ((e = wfpt::trace_prepare()) != cudaSuccess) return e;
+        GraphKey key = make_key(pixels, frame_pixels, s);
+        if (!graph_valid || std::memcmp(&key, &graph_key, sizeof(key)) != 0) {
+            if (graph_exec) cudaGraphExecDestroy(graph_exec);
+            if (graph) cudaGraphDestroy(graph);
+            graph_exec = nullptr;
+            graph = nullptr;
+            graph_valid = false;
+            uint64_t k0 = wfpt::launch_count();
+            if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+            cudaError_t fe = frame(s2w, eye, zfar, pixels, frame_pixels, s, fp_dev);
+            e = cudaStreamEndCapture(s, &graph);
+            if (fe != cudaSuccess) return fe;
+            if (e != cudaSuccess) return e;
+            graph_kernels = wfpt::launch_count() - k0;
+            if ((e = cudaGraphInstantiate(&graph_exec, graph, 0)) != cudaSuccess) return e;
+            graph_key = key;
+            graph_valid = true;
+        }
+        // The parameter block is copied from pageable host memory, which is
+        // staged before the call returns.
+        wfpt::FrameParams hp;
+        std::memset(&hp, 0, sizeof(hp));
+        for (int i = 0; i < 16; ++i) hp.s2w[i] = s2w[i];
+        for (int i = 0; i < 3; ++i) hp.eye[i] = eye[i];
+        hp.zfar = zfar;
+        hp.frame_index = frame_index;
+        if ((e = cudaMemcpyAsync(fp_dev, &hp, sizeof(hp), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaGraphLaunch(graph_exec, s)) != cudaSuccess) return e;
+        wfpt::count_launch((uint32_t)graph_kernels);
+        return cudaSuccess;
+    }
 
     ~wfpt_renderer() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
+        if (fp_dev) cudaFree(fp_dev);
         for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters}) b->release();
         primary.release();
         shadow.release();
@@ -230,12 +301,13 @@ struct wfpt_renderer {
     }
 
     // Renderer::primaryPass (Renderer.cpp:124-131).
-    cudaError_t primary_pass(const float* s2w, const float* eye, float zfar, int pass, float* target, cudaStream_t s) {
+    cudaError_t primary_pass(const float* s2w, const float* eye, float zfar, int pass, float* target, cudaStream_t s,
+                             const wfpt::FrameParams* fp) {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
         int sample_index = pass + cfg.num_primary_samples * (frame_index - 1);
         if ((e = wfpt::launch_raygen_primary(s2w, i2p.as<int32_t>(), primary.rays_cur(), eye, sample_index, width,
-                                             height, zfar, s)) != cudaSuccess)
+                                             height, zfar, s, fp, pass, cfg.num_primary_samples)) != cudaSuccess)
             return e;
         if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), cfg.bvh_kind, primary.rays_cur(),
                                     primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s)) != cudaSuccess)
@@ -249,27 +321,31 @@ struct wfpt_renderer {
                                                cfg.num_primary_samples, s);
     }
 
+    // One frame.  fp (nullable): device-side frame parameters that replace
+    // s2w/eye/zfar/frame_index, so that the same launches can be captured
+    // once into a graph and replayed every frame.  (The reference also
+    // clears `pixels` on frame 1; interpolateColors overwrites all of it on
+    // frame 1, so that clear is not needed.)
     cudaError_t frame(const float* s2w, const float* eye, float zfar, float* pixels, float* frame_pixels,
-                      cudaStream_t s) {
+                      cudaStream_t s, const wfpt::FrameParams* fp = nullptr) {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
         primary.swapped = queue[0].swapped = queue[1].swapped = shadow.swapped = false;
         if ((e = cudaMemsetAsync(frame_pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
-        if (frame_index == 1 && (e = cudaMemsetAsync(pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(counters.p, 0, (size_t)cfg.num_primary_samples * kCountersPerPass * 4, s)) !=
             cudaSuccess)
             return e;
         int rt = cfg.ray_type;
         if (rt == WFPT_PATH_RAYS || rt == WFPT_SHADOW_RAYS)
-            if ((e = wfpt::launch_init_seeds(seeds.as<uint32_t>(), n, frame_index, s)) != cudaSuccess) return e;
+            if ((e = wfpt::launch_init_seeds(seeds.as<uint32_t>(), n, frame_index, s, fp)) != cudaSuccess) return e;
         for (int pass = 0; pass < cfg.num_primary_samples; ++pass) {
             if (rt == WFPT_PRIMARY_RAYS) {
-                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s)) != cudaSuccess) return e;
+                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp)) != cudaSuccess) return e;
                 continue;
             }
             // renderShadow / renderPath (Renderer.cpp:168-199).
             if ((e = cudaMemsetAsync(aux.p, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
-            if ((e = primary_pass(s2w, eye, zfar, pass, aux.as<float>(), s)) != cudaSuccess) return e;
+            if ((e = primary_pass(s2w, eye, zfar, pass, aux.as<float>(), s, fp)) != cudaSuccess) return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
                                  aux.as<float>(), frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s)) !=
                 cudaSuccess)
@@ -316,7 +392,8 @@ struct wfpt_renderer {
                 qsel ^= 1;  // PathQueue::swap
             }
         }
-        return wfpt::launch_interpolate_colors(frame_pixels, pixels, n, frame_index, cfg.key_value, cfg.white_point, s);
+        return wfpt::launch_interpolate_colors(frame_pixels, pixels, n, frame_index, cfg.key_value, cfg.white_point, s,
+                                               fp);
     }
 };
 
@@ -441,8 +518,11 @@ wfpt_status wfpt_renderer_render(wfpt_renderer* r, const wfpt_camera* camera, in
         return WFPT_ERR_INVALID_ARGUMENT;
     }
     if ((e = cudaEventRecord(r->ev0, s)) != cudaSuccess) return wfpt::from_cuda(e);
-    if ((e = r->frame(s2w, camera->position, camera->zfar, pixels, frame_pixels, s)) != cudaSuccess)
-        return wfpt::from_cuda(e);
+    if (r->cfg.use_graph)
+        e = r->render_graph(s2w, camera->position, camera->zfar, pixels, frame_pixels, s);
+    else
+        e = r->frame(s2w, camera->position, camera->zfar, pixels, frame_pixels, s);
+    if (e != cudaSuccess) return wfpt::from_cuda(e);
     if ((e = cudaEventRecord(r->ev1, s)) != cudaSuccess) return wfpt::from_cuda(e);
     size_t cbytes = (size_t)r->cfg.num_primary_samples * kCountersPerPass * 4;
     if ((e = cudaMemcpyAsync(r->host_counters, r->counters.p, cbytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)

@@ -254,6 +254,26 @@ __global__ void k_copy_back(const K* __restrict__ ks, const uint32_t* __restrict
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+template <typename K>
+static size_t onesweep_smem() {
+    constexpr int TILE = tile_of<K>();
+    return (size_t)TILE * sizeof(K) + (size_t)TILE * 4 + (size_t)(kSortWarps + 2) * kRadix * 4;
+}
+
+// Opts the pass kernels into their dynamic shared memory once (not a stream
+// operation, so the renderer calls it before capturing a frame graph).
+cudaError_t sort_prepare() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_onesweep<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)onesweep_smem<uint32_t>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_onesweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)onesweep_smem<uint64_t>());
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 struct SortLayout {
     int passes;
     size_t key_bytes;
@@ -301,14 +321,8 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
 
-    constexpr int TILE = tile_of<K>();
-    size_t smem = (size_t)TILE * sizeof(K) + (size_t)TILE * 4 + (size_t)(kSortWarps + 2) * kRadix * 4;
-    static bool attr_set = false;
-    if (!attr_set) {
-        e = cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    size_t smem = onesweep_smem<K>();
+    if ((e = sort_prepare()) != cudaSuccess) return e;
     K* src_k = keys;
     uint32_t* src_v = values;
     K* dst_k = alt_keys;

@@ -30,8 +30,12 @@ __device__ __forceinline__ uint32_t tea(uint32_t v0, uint32_t v1, uint32_t round
     return v0;
 }
 
-__global__ void k_init_seeds(uint32_t* __restrict__ seeds, uint32_t n, uint32_t frame) {
+// fp (nullable): when given, the frame index comes from the device-side
+// frame parameters of a captured frame graph.
+__global__ void k_init_seeds(uint32_t* __restrict__ seeds, uint32_t n, uint32_t frame,
+                             const FrameParams* __restrict__ fp) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fp) frame = (uint32_t)fp->frame_index;
     if (i < n) seeds[i] = tea(i, frame, 16);
 }
 
@@ -53,13 +57,25 @@ struct Mat4 {
     float m[16];  // column-major, m[c*4 + r]
 };
 
-// raygenPrimary.comp:57-84.
+// raygenPrimary.comp:57-84.  fp (nullable): camera, far plane and sample
+// index (pass + spp * (frame_index - 1)) come from the device-side frame
+// parameters of a captured frame graph instead of the arguments.
 __global__ void k_raygen_primary(Mat4 s2w, const int32_t* __restrict__ index_to_pixel,
                                  float4* __restrict__ rays, float ox, float oy, float oz,
-                                 int sample_index, int width, int height, float max_dist) {
+                                 int sample_index, int width, int height, float max_dist,
+                                 const FrameParams* __restrict__ fp, int pass, int spp) {
     uint32_t task = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t num_pixels = (uint32_t)width * (uint32_t)height;
     if (task >= num_pixels) return;
+    if (fp) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) s2w.m[k] = fp->s2w[k];
+        ox = fp->eye[0];
+        oy = fp->eye[1];
+        oz = fp->eye[2];
+        max_dist = fp->zfar;
+        sample_index = pass + spp * (fp->frame_index - 1);
+    }
     int pixel = index_to_pixel[task];
     int sx = pixel % width;
     int sy = pixel / width;
@@ -452,9 +468,11 @@ __device__ __forceinline__ f3 tonemap_reinhard(f3 c, float key, float white) {
 
 // interpolateColors.comp:78-97.
 __global__ void k_interpolate_colors(float4* __restrict__ frame_pixels, float4* __restrict__ pixels,
-                                     uint32_t n, int frame_index, float key, float white) {
+                                     uint32_t n, int frame_index, float key, float white,
+                                     const FrameParams* __restrict__ fp) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (fp) frame_index = fp->frame_index;
     if (frame_index > 1) {
         float4 p0 = pixels[i];
         float4 p1 = frame_pixels[i];
@@ -489,21 +507,23 @@ __global__ void k_fill_u32(uint32_t* __restrict__ dst, uint32_t v, size_t n) {
 // ------------------------------------------------------------ launchers
 static inline unsigned grid_for(uint64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
-cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s) {
+cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s, const FrameParams* fp) {
     if (n == 0) return cudaSuccess;
-    k_init_seeds<<<grid_for(n), kBlock, 0, s>>>(seeds, n, (uint32_t)frame);
+    k_init_seeds<<<grid_for(n), kBlock, 0, s>>>(seeds, n, (uint32_t)frame, fp);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_raygen_primary(const float* m, const int32_t* i2p, wfpt_ray* rays, const float* o,
-                                  int sample_index, int w, int h, float max_dist, cudaStream_t s) {
+                                  int sample_index, int w, int h, float max_dist, cudaStream_t s,
+                                  const FrameParams* fp, int pass, int spp) {
     uint64_t n = (uint64_t)w * (uint64_t)h;
     if (n == 0) return cudaSuccess;
     Mat4 mm;
-    for (int i = 0; i < 16; ++i) mm.m[i] = m[i];
-    k_raygen_primary<<<grid_for(n), kBlock, 0, s>>>(mm, i2p, reinterpret_cast<float4*>(rays), o[0], o[1],
-                                                    o[2], sample_index, w, h, max_dist);
+    for (int i = 0; i < 16; ++i) mm.m[i] = m ? m[i] : 0.0f;
+    float oo[3] = {o ? o[0] : 0.0f, o ? o[1] : 0.0f, o ? o[2] : 0.0f};
+    k_raygen_primary<<<grid_for(n), kBlock, 0, s>>>(mm, i2p, reinterpret_cast<float4*>(rays), oo[0], oo[1],
+                                                    oo[2], sample_index, w, h, max_dist, fp, pass, spp);
     count_launch();
     return cudaGetLastError();
 }
@@ -576,11 +596,11 @@ cudaError_t launch_count_hits(const wfpt_hit* res, uint32_t n, const uint32_t* n
 }
 
 cudaError_t launch_interpolate_colors(float* frame_pixels, float* pixels, uint32_t n, int frame_index,
-                                      float key, float white, cudaStream_t s) {
+                                      float key, float white, cudaStream_t s, const FrameParams* fp) {
     if (n == 0) return cudaSuccess;
     k_interpolate_colors<<<grid_for(n), kBlock, 0, s>>>(reinterpret_cast<float4*>(frame_pixels),
                                                         reinterpret_cast<float4*>(pixels), n, frame_index,
-                                                        key, white);
+                                                        key, white, fp);
     count_launch();
     return cudaGetLastError();
 }

@@ -9,6 +9,16 @@
 
 namespace wfpt {
 
+// Per-frame values read on the device by a captured frame graph (updated by
+// one host-to-device copy before each launch).
+struct FrameParams {
+    float s2w[16];      // inverse(P * V), column-major
+    float eye[3];
+    float zfar;
+    int frame_index;    // Renderer::frameIndex (1-based)
+    int pad[3];
+};
+
 // Number of kernels this library has launched (all threads, all devices).
 void count_launch(uint32_t k = 1);
 uint64_t launch_count();
@@ -18,9 +28,11 @@ cudaError_t status_stages(uint32_t* out);
 cudaError_t status_sort(uint32_t* out);
 cudaError_t status_trace(uint32_t* out);
 
-cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s);
+cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s,
+                              const FrameParams* fp = nullptr);
 cudaError_t launch_raygen_primary(const float* m, const int32_t* i2p, wfpt_ray* rays, const float* o,
-                                  int sample_index, int w, int h, float max_dist, cudaStream_t s);
+                                  int sample_index, int w, int h, float max_dist, cudaStream_t s,
+                                  const FrameParams* fp = nullptr, int pass = 0, int spp = 1);
 cudaError_t launch_raygen_shadow(const uint32_t* seeds, const wfpt_ray* in_rays, const wfpt_hit* in_res,
                                  wfpt_ray* out_rays, int32_t* s2i, int32_t* i2s, const float* light,
                                  float radius, int bb, int bs, const uint32_t* n_in_dev, int S,
@@ -41,7 +53,10 @@ cudaError_t launch_reconstruct_shadow(const wfpt_hit* res, const int32_t* i2p, c
 cudaError_t launch_count_hits(const wfpt_hit* res, uint32_t n, const uint32_t* n_dev, uint32_t* count,
                               cudaStream_t s);
 cudaError_t launch_interpolate_colors(float* frame_pixels, float* pixels, uint32_t n, int frame_index,
-                                      float key, float white, cudaStream_t s);
+                                      float key, float white, cudaStream_t s, const FrameParams* fp = nullptr);
+// Host-side one-time set-up that must not happen inside a stream capture
+// (function attributes, occupancy queries).
+cudaError_t sort_prepare();
 cudaError_t launch_fill_u32(void* dst, uint32_t v, size_t n, cudaStream_t s);
 cudaError_t launch_batch_count(const uint32_t* n_in_dev, uint32_t begin, uint32_t size, int S, uint32_t* out,
                                cudaStream_t s);

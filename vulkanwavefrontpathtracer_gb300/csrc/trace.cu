@@ -505,6 +505,21 @@ static bool g_count = false;
 void set_trace_count(bool on) { g_count = on; }
 bool get_trace_count() { return g_count; }
 
+// SM count and resident blocks of the persistent kernel (host queries that
+// must not run inside a stream capture; the renderer calls this first).
+cudaError_t trace_prepare() {
+    if (g_num_sms != 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false, false>, kBlock, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true, false>, kBlock, 0);
+    if (e == cudaSuccess) g_num_sms = sms;
+    return e;
+}
+
 cudaError_t trace_counters(uint64_t out[4], bool reset) {
     unsigned long long v[4];
     cudaError_t e = cudaMemcpyFromSymbol(v, g_counts, sizeof(v));
@@ -527,11 +542,8 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
     int4* out = reinterpret_cast<int4*>(results);
     if (kind == WFPT_BVH8_Q8) {
         if (g_num_sms == 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false, false>, kBlock, 0);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true, false>, kBlock, 0);
+            cudaError_t e = trace_prepare();
+            if (e != cudaSuccess) return e;
         }
         unsigned pgrid = (unsigned)(g_num_sms * (closest ? g_blocks_per_sm[1] : g_blocks_per_sm[0]));
         if (pgrid == 0) pgrid = 1;

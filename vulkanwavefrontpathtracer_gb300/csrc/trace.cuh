@@ -22,6 +22,7 @@ uint32_t get_trace_postpone();
 void set_trace_count(bool on);
 bool get_trace_count();
 cudaError_t trace_counters(uint64_t out[4], bool reset);
+cudaError_t trace_prepare();
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
