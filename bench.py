@@ -46,9 +46,9 @@ COURTYARD = dict(
 # Shadow rays are generated in the (already reordered) slot order of their
 # path rays and all aim at the light, so the chosen form does not sort them.
 CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=0,
-              reorder_shadow_rays=0)
+              reorder_shadow_rays=0, use_graph=1)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
-             reorder_shadow_rays=0)
+             reorder_shadow_rays=0, use_graph=1)
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"

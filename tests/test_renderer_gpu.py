@@ -122,3 +122,37 @@ def test_accumulation_over_frames_and_spp(wf, orc, dev, small):
     px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 40, 40, frames=3, num_primary_samples=2,
                                             sort_path_rays=1, reorder_path_rays=1)
     assert same_bits(fp, o_fp) and same_bits(px, o_px)
+
+
+@pytest.mark.parametrize("opts", [
+    dict(),
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1),
+    dict(ray_type=1, sort_shadow_rays=1, reorder_shadow_rays=1),
+])
+def test_graph_frames_match_direct_frames(wf, dev, small, opts):
+    """use_graph=1 replays one captured frame with the camera and frame
+    index read from device memory; frames must equal directly launched ones
+    while the camera moves and the frame index advances."""
+    import torch
+    sc, geom, nodes, tris, hg = small
+    base = dict(ray_type=wf.PATH_RAYS, num_primary_samples=1, num_shadow_samples=2, shadow_radius=0.1,
+                recursion_depth=4, key_value=0.6, white_point=2.0, bvh_kind=wf.BVH2_FP32, albedo=0.8)
+    base.update(opts)
+    w, h = 72, 48
+    outs = []
+    for use_graph in (0, 1):
+        r = wf.api.Renderer(use_graph=use_graph, **base)
+        r.set_scene(sc, geom, LIGHT, BG)
+        px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+        fp = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+        seq = []
+        for f in range(4):
+            cam = wf.api.make_camera(**dict(CAM, position=(0.5 + 0.05 * (f % 2), 0.5, 2.2)))
+            r.render(cam, w, h, px, fp)
+            st = r.stats()
+            seq.append((N(px).copy(), N(fp).copy(), st.num_path_rays, st.num_shadow_rays))
+        outs.append(seq)
+    assert wf.api.device_status() == 0
+    for (pa, fa, na, sa), (pb, fb, nb, sb) in zip(*outs):
+        assert na == nb and sa == sb
+        assert same_bits(pa, pb) and same_bits(fa, fb)

@@ -107,8 +107,10 @@ struct wfpt_renderer {
     bool stats_pending = false;
     float frame_ms = 0.0f;
 
-    // Frame graph: captured once per (configuration, resolution, buffers,
-    // stream); replayed with the per-frame values in fp_dev.
+    // Frame graph: captured once per (configuration, resolution, buffers)
+    // on a private stream (the legacy default stream cannot be captured);
+    // replayed on the caller's stream with the per-frame values in fp_dev.
+    cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     wfpt::FrameParams* fp_dev = nullptr;
@@ -116,12 +118,12 @@ struct wfpt_renderer {
     struct GraphKey {
         wfpt_renderer_config cfg;
         int w, h;
-        const void *pixels, *frame_pixels, *stream, *scene, *geoms;
+        const void *pixels, *frame_pixels, *scene, *geoms;
         float light[3], bg[3], smin[3], smax[3];
     } graph_key{};
     bool graph_valid = false;
 
-    GraphKey make_key(float* pixels, float* frame_pixels, cudaStream_t s) const {
+    GraphKey make_key(float* pixels, float* frame_pixels) const {
         GraphKey k;
         std::memset(&k, 0, sizeof(k));
         k.cfg = cfg;
@@ -129,7 +131,6 @@ struct wfpt_renderer {
         k.h = height;
         k.pixels = pixels;
         k.frame_pixels = frame_pixels;
-        k.stream = s;
         k.scene = scene;
         k.geoms = geoms;
         for (int i = 0; i < 3; ++i) {
@@ -146,9 +147,11 @@ struct wfpt_renderer {
                              cudaStream_t s) {
         cudaError_t e;
         if (!fp_dev && (e = cudaMalloc(&fp_dev, sizeof(wfpt::FrameParams))) != cudaSuccess) return e;
+        if (!capture_stream && (e = cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return e;
         if ((e = wfpt::sort_prepare()) != cudaSuccess) return e;
         if ((e = wfpt::trace_prepare()) != cudaSuccess) return e;
-        GraphKey key = make_key(pixels, frame_pixels, s);
+        GraphKey key = make_key(pixels, frame_pixels);
         if (!graph_valid || std::memcmp(&key, &graph_key, sizeof(key)) != 0) {
             if (graph_exec) cudaGraphExecDestroy(graph_exec);
             if (graph) cudaGraphDestroy(graph);
@@ -156,9 +159,10 @@ struct wfpt_renderer {
             graph = nullptr;
             graph_valid = false;
             uint64_t k0 = wfpt::launch_count();
-            if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-            cudaError_t fe = frame(s2w, eye, zfar, pixels, frame_pixels, s, fp_dev);
-            e = cudaStreamEndCapture(s, &graph);
+            const cudaStream_t cs = capture_stream;
+            if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+            cudaError_t fe = frame(s2w, eye, zfar, pixels, frame_pixels, cs, fp_dev);
+            e = cudaStreamEndCapture(cs, &graph);
             if (fe != cudaSuccess) return fe;
             if (e != cudaSuccess) return e;
             graph_kernels = wfpt::launch_count() - k0;
@@ -184,6 +188,7 @@ struct wfpt_renderer {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
         if (fp_dev) cudaFree(fp_dev);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
         for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters}) b->release();
         primary.release();
         shadow.release();
