@@ -225,6 +225,44 @@ wfpt_status wfpt_raygen_path(uint32_t* seeds, const wfpt_geometry* geometries,
                              float albedo, void* scratch, size_t scratch_bytes,
                              void* stream);
 
+/* Largest n accepted by wfpt_raygen_path_static. */
+#define WFPT_RAYGEN_PATH_STATIC_MAX_RAYS 16777216u
+
+/* wfpt_raygen_path without caller scratch; no counterpart in the reference
+ * (the reference's raygenPath.comp appends through an atomic counter and
+ * needs no scratch).
+ *
+ * For callers that cannot hand the library device memory: an engine whose
+ * device memory is all owned by its own allocator (for example a Vulkan
+ * renderer that exports a fixed set of buffers to CUDA and has none spare),
+ * or code on a latency-critical path where cudaMalloc / cudaFree would
+ * synchronise the device.  This call allocates nothing: its compaction
+ * scratch is a fixed 256 KiB array in the library's device image
+ * (one per device), enough for n <= WFPT_RAYGEN_PATH_STATIC_MAX_RAYS.
+ *
+ * - Results equal wfpt_raygen_path's for the same inputs.
+ * - n above WFPT_RAYGEN_PATH_STATIC_MAX_RAYS is rejected with
+ *   WFPT_ERR_INVALID_ARGUMENT before anything is launched; use
+ *   wfpt_raygen_path with caller scratch for larger wavefronts.
+ * - The tile ticket and the per-tile look-back states must start at zero;
+ *   the call clears them itself, stream-ordered on `stream`, before its
+ *   kernel.  The caller clears nothing.  *out_count_dev is written, not
+ *   accumulated.
+ * - The first call on each device looks up the array's device address with
+ *   that device current; make that first call outside any stream capture.
+ * - All calls on one device share the one array: calls that overlap in time
+ *   (two streams with no event ordering them, or two host threads) race on
+ *   it and give wrong output or WFPT_ERR_TIMEOUT from wfpt_device_status.
+ *   Issue them on one stream or order them with events. */
+wfpt_status wfpt_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geometries,
+                                    const wfpt_ray* in_rays, wfpt_ray* out_rays,
+                                    const int32_t* in_index_to_pixel,
+                                    int32_t* out_index_to_pixel,
+                                    const wfpt_hit* in_results, float* decreases,
+                                    uint32_t* out_count_dev, uint32_t n,
+                                    const uint32_t* n_dev, int russian_roulette,
+                                    float albedo, void* stream);
+
 /* reconstructSmooth.comp:34-96 + Renderer::reconstructSmooth
  * (Renderer.cpp:201-223).  pixels/decreases are float4 per pixel. */
 wfpt_status wfpt_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* results,

@@ -50,6 +50,9 @@ def test_invalid_arguments_rejected_on_host(wf):
                                   None) == 1
     assert lib.wfpt_trace(None, 0, buf, buf, None, 4, None, 1, None) == 1
     assert b"null" in lib.wfpt_last_error_message()
+    big = wf.api.RAYGEN_PATH_STATIC_MAX_RAYS + 1
+    assert lib.wfpt_raygen_path_static(buf, buf, buf, buf, buf, buf, buf, buf, buf, big, None, 0, 0.8, None) == 1
+    assert b"WFPT_RAYGEN_PATH_STATIC_MAX_RAYS" in lib.wfpt_last_error_message()
 
 
 def test_pixel_table_matches_oracle(wf, orc):

@@ -127,6 +127,8 @@ _SIGS = {
     "wfpt_raygen_path_scratch_bytes": (c_size_t, [c_u32]),
     "wfpt_raygen_path": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p, c_u32, c_void_p, c_int, c_float, c_void_p, c_size_t, c_void_p]),
+    "wfpt_raygen_path_static": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p, c_u32, c_void_p, c_int, c_float, c_void_p]),
     "wfpt_reconstruct_smooth": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P_f32, P_f32,
                                         c_u32, c_void_p, c_int, c_void_p]),
     "wfpt_reconstruct_shadow": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,

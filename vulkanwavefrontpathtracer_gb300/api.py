@@ -149,6 +149,20 @@ def raygen_path(seeds, geometries, in_rays, out_rays, in_index_to_pixel, out_ind
     return scratch
 
 
+RAYGEN_PATH_STATIC_MAX_RAYS = 16777216
+
+
+def raygen_path_static(seeds, geometries, in_rays, out_rays, in_index_to_pixel, out_index_to_pixel, in_results,
+                       decreases, out_count, n=None, n_dev=None, albedo=0.8, russian_roulette=False, stream=None):
+    """raygen_path over the library's own fixed scratch: allocates nothing.
+    n at most RAYGEN_PATH_STATIC_MAX_RAYS; calls on one device must not
+    overlap in time (they share the scratch)."""
+    L.check(lib().wfpt_raygen_path_static(_p(seeds), _p(geometries), _p(in_rays), _p(out_rays),
+                                          _p(in_index_to_pixel), _p(out_index_to_pixel), _p(in_results),
+                                          _p(decreases), _p(out_count), _n(in_rays, n), _p(n_dev),
+                                          1 if russian_roulette else 0, albedo, _s(stream)))
+
+
 def reconstruct_smooth(rays, results, index_to_pixel, pixels, decreases, geometries, light, background,
                        num_samples, n=None, n_dev=None, stream=None):
     L.check(lib().wfpt_reconstruct_smooth(_p(rays), _p(results), _p(index_to_pixel), _p(pixels), _p(decreases),

@@ -267,6 +267,23 @@ wfpt_status wfpt_raygen_path(uint32_t* seeds, const wfpt_geometry* geometries, c
                                               albedo, scratch, S(stream)));
 }
 
+wfpt_status wfpt_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geometries, const wfpt_ray* in_rays,
+                                    wfpt_ray* out_rays, const int32_t* in_index_to_pixel,
+                                    int32_t* out_index_to_pixel, const wfpt_hit* in_results, float* decreases,
+                                    uint32_t* out_count_dev, uint32_t n, const uint32_t* n_dev,
+                                    int russian_roulette, float albedo, void* stream) {
+    (void)russian_roulette;
+    WFPT_REQUIRE(n <= WFPT_RAYGEN_PATH_STATIC_MAX_RAYS,
+                 "n exceeds WFPT_RAYGEN_PATH_STATIC_MAX_RAYS (16777216); use wfpt_raygen_path with caller scratch");
+    WFPT_REQUIRE(out_count_dev, "null counter");
+    WFPT_REQUIRE(n == 0 || (seeds && geometries && in_rays && out_rays && in_index_to_pixel && out_index_to_pixel &&
+                            in_results && decreases),
+                 "null buffer");
+    return from_cuda(wfpt::launch_raygen_path_static(seeds, geometries, in_rays, out_rays, in_index_to_pixel,
+                                                     out_index_to_pixel, in_results, decreases, out_count_dev, n,
+                                                     n_dev, albedo, S(stream)));
+}
+
 wfpt_status wfpt_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* results, const int32_t* index_to_pixel,
                                     float* pixels, const float* decreases, const wfpt_geometry* geometries,
                                     const float light[3], const float background[3], uint32_t n,

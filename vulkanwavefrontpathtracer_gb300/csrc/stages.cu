@@ -6,6 +6,7 @@
 // item, 256-thread blocks; every kernel honours an optional device-side
 // element count so that a frame can run without host readbacks.
 #include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 #include "stages.cuh"
@@ -559,6 +560,58 @@ cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, cons
         seeds, geoms, reinterpret_cast<const float4*>(in_rays), reinterpret_cast<float4*>(out_rays), in_i2p,
         out_i2p, reinterpret_cast<const int4*>(in_res), reinterpret_cast<float4*>(decreases), out_count, n,
         n_dev, albedo, reinterpret_cast<uint32_t*>(scratch));
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Library-owned compaction scratch for launch_raygen_path_static: the tile
+// ticket (word 0) and one look-back state per 256-ray tile (words 1..),
+// for at most WFPT_RAYGEN_PATH_STATIC_MAX_RAYS rays; 65,537 words (256 KiB)
+// per device, placed by the module loader, never by an allocation call.
+constexpr size_t kPathStaticWords = 1 + (WFPT_RAYGEN_PATH_STATIC_MAX_RAYS + kBlock - 1) / kBlock;
+static __device__ __align__(256) uint32_t g_path_static_scratch[kPathStaticWords];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_path_static_mu;
+uint32_t* g_path_static_ptr[kMaxDevices] = {};
+
+// Device address of g_path_static_scratch on the current device, looked up
+// once per device (cudaGetSymbolAddress, with that device current).
+cudaError_t path_static_scratch(uint32_t** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_path_static_mu);
+    if (!g_path_static_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_path_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_path_static_ptr[dev] = static_cast<uint32_t*>(p);
+    }
+    *out = g_path_static_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geoms, const wfpt_ray* in_rays,
+                                      wfpt_ray* out_rays, const int32_t* in_i2p, int32_t* out_i2p,
+                                      const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
+                                      uint32_t n, const uint32_t* n_dev, float albedo, cudaStream_t s) {
+    if (n > WFPT_RAYGEN_PATH_STATIC_MAX_RAYS) return cudaErrorInvalidValue;
+    uint32_t* scratch = nullptr;
+    cudaError_t e = path_static_scratch(&scratch);
+    if (e != cudaSuccess) return e;
+    // The ticket and the tile states of this call's tiles start at zero.
+    size_t tiles = ((size_t)n + kBlock - 1) / kBlock;
+    e = cudaMemsetAsync(scratch, 0, (1 + tiles) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    unsigned grid = tiles == 0 ? 1u : (unsigned)tiles;
+    k_raygen_path<<<grid, kBlock, 0, s>>>(
+        seeds, geoms, reinterpret_cast<const float4*>(in_rays), reinterpret_cast<float4*>(out_rays), in_i2p,
+        out_i2p, reinterpret_cast<const int4*>(in_res), reinterpret_cast<float4*>(decreases), out_count, n,
+        n_dev, albedo, scratch);
     count_launch();
     return cudaGetLastError();
 }

@@ -43,6 +43,12 @@ cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, cons
                                const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
                                uint32_t n, const uint32_t* n_dev, float albedo, void* scratch,
                                cudaStream_t s);
+// launch_raygen_path over the library's static scratch (n at most
+// WFPT_RAYGEN_PATH_STATIC_MAX_RAYS); calls on one device must not overlap.
+cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geoms, const wfpt_ray* in_rays,
+                                      wfpt_ray* out_rays, const int32_t* in_i2p, int32_t* out_i2p,
+                                      const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
+                                      uint32_t n, const uint32_t* n_dev, float albedo, cudaStream_t s);
 cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res, const int32_t* i2p,
                                       float* pixels, const float* decreases, const wfpt_geometry* geoms,
                                       const float* light, const float* bg, uint32_t n,
