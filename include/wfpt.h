@@ -123,7 +123,12 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          are idle (1..32, default 8)
  *   "trace.bvh8.postpone"  postpone a node's triangle tests while fewer than
  *                          this many lanes have triangles (0..32, 0 = off)
- *   "trace.count"          1 = launch the counting traversal kernels, which
+ *   "trace.bvh8.coop"      1 = the warp tests all of its lanes' pending
+ *                          triangles together, 32 at a time (default);
+ *                          0 = each lane tests its own.  Closest hits are
+ *                          identical; an any-hit ray may report a different
+ *                          (equally valid) occluder
+ *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */
 wfpt_status wfpt_tune_set(const char* key, int64_t value);

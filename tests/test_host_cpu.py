@@ -131,6 +131,23 @@ def test_bvh2_is_valid(wf):
     assert seen == 3000
 
 
+@pytest.mark.parametrize("ntris", [0, 1, 2, 9])
+def test_tiny_and_empty_scenes_build(wf, ntris):
+    """Scene creation for empty and few-triangle scenes (the empty BVHs
+    carry one placeholder record)."""
+    pos = np.arange(3 * 3 * max(ntris, 1), dtype=np.float32).reshape(-1, 3) * 0.1
+    pos[:, 1] = np.sin(pos[:, 0])
+    idx = np.arange(3 * ntris, dtype=np.uint32).reshape(-1, 3)
+    sc = wf.api.Scene(pos, idx, host_only=True)
+    nodes_u8, tris_u8 = sc.export_bvh8()
+    ids = tris_u8.view(np.uint32).reshape(-1, 12)[:, 11]
+    if ntris:
+        assert sorted(ids.tolist()) == list(range(ntris))
+    else:
+        assert ids.shape[0] == 1
+    sc.close()
+
+
 def test_bvh8_boxes_are_conservative(wf):
     pos, _, idx = wf.api.generate_scene(0, 4, 4000)
     sc = wf.api.Scene(pos, idx, host_only=True)
@@ -222,15 +239,19 @@ def test_cpu_frame_runs(wf, orc):
 
 def test_tuning_knobs(wf):
     api = wf.api
-    old = api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone")
+    old = api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"), api.tune_get("trace.bvh8.coop")
+    assert old[2] == 1  # cooperative triangle tests on by default
     try:
         api.tune_set("trace.bvh8.refill", 4)
         api.tune_set("trace.bvh8.postpone", 6)
+        api.tune_set("trace.bvh8.coop", 0)
         assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
+        assert api.tune_get("trace.bvh8.coop") == 0
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
-                         ("no.such.knob", 1)):
+                         ("trace.bvh8.coop", 2), ("no.such.knob", 1)):
             with pytest.raises(wf.WfptError):
                 api.tune_set(key, bad)
     finally:
         api.tune_set("trace.bvh8.refill", old[0])
         api.tune_set("trace.bvh8.postpone", old[1])
+        api.tune_set("trace.bvh8.coop", old[2])

@@ -146,19 +146,58 @@ def test_multi_geometry_ids(wf, dev):
     assert np.all(hit[hit[:, 1] == 1, 0] < 1500) and np.all(hit[hit[:, 1] == 2, 0] < 500)
 
 
+@pytest.mark.parametrize("coop", [0, 1])
 @pytest.mark.parametrize("refill,postpone", [(1, 0), (32, 0), (8, 8), (4, 16)])
-def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone):
+def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone, coop):
     pos, idx, sc = soup
     rays = random_rays(np.random.default_rng(12), 60000)
     ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
     ref_any = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=False)
-    old = wf.api.tune_get("trace.bvh8.refill"), wf.api.tune_get("trace.bvh8.postpone")
+    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop")
+    old = [wf.api.tune_get(k) for k in keys]
     try:
-        wf.api.tune_set("trace.bvh8.refill", refill)
-        wf.api.tune_set("trace.bvh8.postpone", postpone)
+        for k, v in zip(keys, (refill, postpone, coop)):
+            wf.api.tune_set(k, v)
         assert np.array_equal(gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays), ref)
         a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)
         assert np.array_equal(a8[:, 0] >= 0, ref_any[:, 0] >= 0)
+        hit = a8[:, 0] >= 0
+        # An any-hit result is a genuine hit: same record layout, t inside
+        # the ray interval.
+        t = a8[hit, 2].view(np.float32)
+        assert np.all((t >= rays[hit, 3]) & (t <= rays[hit, 7]))
     finally:
-        wf.api.tune_set("trace.bvh8.refill", old[0])
-        wf.api.tune_set("trace.bvh8.postpone", old[1])
+        for k, v in zip(keys, old):
+            wf.api.tune_set(k, v)
+    assert wf.api.device_status() == 0
+
+
+def test_bvh8_coop_courtyard_and_ties(wf, dev, courtyard):
+    """Cooperative and per-lane triangle tests give identical closest hits
+    on the courtyard, including rays that start on a triangle (tmin 0) and
+    rays through shared edges."""
+    pos, idx, sc = courtyard
+    rng = np.random.default_rng(21)
+    n = 200000
+    tri = rng.integers(0, idx.shape[0], n)
+    v = pos[idx[tri]]  # [n, 3, 3]
+    w = rng.dirichlet((1, 1, 1), n).astype(np.float32)
+    w[: n // 4, 2] = 0.0  # on an edge
+    w[: n // 4] /= w[: n // 4].sum(1, keepdims=True)
+    p = np.einsum("nk,nkd->nd", w, v).astype(np.float32)
+    rays = random_rays(rng, n, tmax=1e30)
+    rays[:, :3] = p
+    rays[n // 2:, :3] -= 3.0 * rays[n // 2:, 4:7]  # in front of the surface, looking at it
+    old = wf.api.tune_get("trace.bvh8.coop")
+    try:
+        wf.api.tune_set("trace.bvh8.coop", 0)
+        lane = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays)
+        wf.api.tune_set("trace.bvh8.coop", 1)
+        coop = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays)
+    finally:
+        wf.api.tune_set("trace.bvh8.coop", old)
+    assert np.array_equal(lane, coop)
+    # Rays aimed at edges from 3 units away: ties between the triangles of
+    # an edge resolve the same way in both BVH forms.
+    front = slice(n // 2, n)
+    assert np.array_equal(coop[front], gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)[front])

@@ -36,29 +36,31 @@ def _timeit(fn: Callable[[], None], reps: int = 5, warm: int = 2) -> float:
 
 
 def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[int] = (1, 2, 4, 8, 16, 32),
-                   postpones: Iterable[int] = (0, 4, 8, 12), reps: int = 5) -> Dict:
-    """Grid search of (refill, postpone) for BVH8 closest-hit and any-hit
-    traversal; returns the best settings and the full table (ms)."""
+                   postpones: Iterable[int] = (0, 4, 8, 12), coops: Iterable[int] = (0, 1), reps: int = 5) -> Dict:
+    """Grid search of (refill, postpone, coop) for BVH8 closest-hit and
+    any-hit traversal; returns the best settings and the full table (ms)."""
     import torch
     dev = closest_rays.device
     res_c = torch.empty((closest_rays.shape[0], 4), dtype=torch.int32, device=dev)
     res_a = torch.empty((any_rays.shape[0], 4), dtype=torch.int32, device=dev)
-    old = (api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"))
+    old = (api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"), api.tune_get("trace.bvh8.coop"))
     table = []
     try:
-        for refill, post in itertools.product(refills, postpones):
+        for refill, post, coop in itertools.product(refills, postpones, coops):
             api.tune_set("trace.bvh8.refill", refill)
             api.tune_set("trace.bvh8.postpone", post)
+            api.tune_set("trace.bvh8.coop", coop)
             mc = _timeit(lambda: api.trace(scene, L.BVH8_Q8, closest_rays, res_c, closest_hit=True), reps)
             ma = _timeit(lambda: api.trace(scene, L.BVH8_Q8, any_rays, res_a, closest_hit=False), reps)
-            table.append({"refill": refill, "postpone": post, "closest_ms": mc, "any_ms": ma})
+            table.append({"refill": refill, "postpone": post, "coop": coop, "closest_ms": mc, "any_ms": ma})
     finally:
         api.tune_set("trace.bvh8.refill", old[0])
         api.tune_set("trace.bvh8.postpone", old[1])
+        api.tune_set("trace.bvh8.coop", old[2])
     # The knobs are shared by both kinds of rays: weigh them by ray count.
     nc, na = closest_rays.shape[0], any_rays.shape[0]
     best = min(table, key=lambda e: e["closest_ms"] + e["any_ms"])
-    return {"refill": best["refill"], "postpone": best["postpone"], "table": table,
+    return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "table": table,
             "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
             "best_any_mrays_s": na / (best["any_ms"] * 1e-3) / 1e6}
 
@@ -123,3 +125,5 @@ def measure_work(scene: api.Scene, rays, bvh_kind: int, closest: bool) -> Dict:
 def apply(traversal: Dict) -> None:
     api.tune_set("trace.bvh8.refill", traversal["refill"])
     api.tune_set("trace.bvh8.postpone", traversal["postpone"])
+    if "coop" in traversal:
+        api.tune_set("trace.bvh8.coop", traversal["coop"])

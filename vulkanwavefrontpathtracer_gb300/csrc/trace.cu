@@ -104,35 +104,41 @@ struct Uvw {
     bool edge_ok;
 };
 
-// Woop-Benthin-Wald edge functions and scaled distance for one triangle.
-__device__ __forceinline__ Uvw tri_uvw(const RayT& r, const float4& a4, const float4& b4, const float4& c4) {
-    f3 A = sub(mk(a4.x, a4.y, a4.z), r.o);
-    f3 B = sub(mk(b4.x, b4.y, b4.z), r.o);
-    f3 C = sub(mk(c4.x, c4.y, c4.z), r.o);
-    float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
-    float Ax = __fsub_rn(comp(A, r.kx), __fmul_rn(r.sx, Akz));
-    float Ay = __fsub_rn(comp(A, r.ky), __fmul_rn(r.sy, Akz));
-    float Bx = __fsub_rn(comp(B, r.kx), __fmul_rn(r.sx, Bkz));
-    float By = __fsub_rn(comp(B, r.ky), __fmul_rn(r.sy, Bkz));
-    float Cx = __fsub_rn(comp(C, r.kx), __fmul_rn(r.sx, Ckz));
-    float Cy = __fsub_rn(comp(C, r.ky), __fmul_rn(r.sy, Ckz));
-    Uvw o;
-    o.U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-    o.V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-    o.W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if (o.U == 0.0f || o.V == 0.0f || o.W == 0.0f) {
+// Woop-Benthin-Wald edge functions and scaled distance for one triangle,
+// from the ray origin, its axis permutation and shear constants.
+__device__ __forceinline__ Uvw tri_uvw(const f3& org, int kx, int ky, int kz, float sx, float sy, float sz,
+                                       const float4& a4, const float4& b4, const float4& c4) {
+    f3 A = sub(mk(a4.x, a4.y, a4.z), org);
+    f3 B = sub(mk(b4.x, b4.y, b4.z), org);
+    f3 C = sub(mk(c4.x, c4.y, c4.z), org);
+    float Akz = comp(A, kz), Bkz = comp(B, kz), Ckz = comp(C, kz);
+    float Ax = __fsub_rn(comp(A, kx), __fmul_rn(sx, Akz));
+    float Ay = __fsub_rn(comp(A, ky), __fmul_rn(sy, Akz));
+    float Bx = __fsub_rn(comp(B, kx), __fmul_rn(sx, Bkz));
+    float By = __fsub_rn(comp(B, ky), __fmul_rn(sy, Bkz));
+    float Cx = __fsub_rn(comp(C, kx), __fmul_rn(sx, Ckz));
+    float Cy = __fsub_rn(comp(C, ky), __fmul_rn(sy, Ckz));
+    Uvw q;
+    q.U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    q.V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    q.W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (q.U == 0.0f || q.V == 0.0f || q.W == 0.0f) {
         double cxby = (double)Cx * (double)By, cybx = (double)Cy * (double)Bx;
-        o.U = (float)(cxby - cybx);
+        q.U = (float)(cxby - cybx);
         double axcy = (double)Ax * (double)Cy, aycx = (double)Ay * (double)Cx;
-        o.V = (float)(axcy - aycx);
+        q.V = (float)(axcy - aycx);
         double bxay = (double)Bx * (double)Ay, byax = (double)By * (double)Ax;
-        o.W = (float)(bxay - byax);
+        q.W = (float)(bxay - byax);
     }
-    o.edge_ok = !((o.U < 0.0f || o.V < 0.0f || o.W < 0.0f) && (o.U > 0.0f || o.V > 0.0f || o.W > 0.0f));
-    o.det = __fadd_rn(__fadd_rn(o.U, o.V), o.W);
-    float Az = __fmul_rn(r.sz, Akz), Bz = __fmul_rn(r.sz, Bkz), Cz = __fmul_rn(r.sz, Ckz);
-    o.T = __fadd_rn(__fadd_rn(__fmul_rn(o.U, Az), __fmul_rn(o.V, Bz)), __fmul_rn(o.W, Cz));
-    return o;
+    q.edge_ok = !((q.U < 0.0f || q.V < 0.0f || q.W < 0.0f) && (q.U > 0.0f || q.V > 0.0f || q.W > 0.0f));
+    q.det = __fadd_rn(__fadd_rn(q.U, q.V), q.W);
+    float Az = __fmul_rn(sz, Akz), Bz = __fmul_rn(sz, Bkz), Cz = __fmul_rn(sz, Ckz);
+    q.T = __fadd_rn(__fadd_rn(__fmul_rn(q.U, Az), __fmul_rn(q.V, Bz)), __fmul_rn(q.W, Cz));
+    return q;
+}
+
+__device__ __forceinline__ Uvw tri_uvw(const RayT& r, const float4& a4, const float4& b4, const float4& c4) {
+    return tri_uvw(r.o, r.kx, r.ky, r.kz, r.sx, r.sy, r.sz, a4, b4, c4);
 }
 
 // Watertight test of record `rec`; on acceptance updates `h`.
@@ -490,16 +496,263 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8(const float4* __restri
     }
 }
 
+// ------------------------------------ BVH8 with warp-cooperative triangles
+// Ray fields the triangle test reads, kept in shared memory so that any
+// lane of the warp can test a triangle against any other lane's ray.
+struct alignas(16) RayS {
+    float ox, oy, oz, tmin;
+    float sx, sy, sz;
+    uint32_t k;  // kx | ky << 2 | kz << 4
+};
+
+__device__ __forceinline__ RayS ray_shared(const RayT& r) {
+    RayS s;
+    s.ox = r.o.x;
+    s.oy = r.o.y;
+    s.oz = r.o.z;
+    s.tmin = r.tmin;
+    s.sx = r.sx;
+    s.sy = r.sy;
+    s.sz = r.sz;
+    s.k = (uint32_t)r.kx | ((uint32_t)r.ky << 2) | ((uint32_t)r.kz << 4);
+    return s;
+}
+
+__device__ __forceinline__ Uvw tri_uvw(const RayS& s, const float4& a4, const float4& b4, const float4& c4) {
+    return tri_uvw(mk(s.ox, s.oy, s.oz), (int)(s.k & 3u), (int)((s.k >> 2) & 3u), (int)(s.k >> 4), s.sx, s.sy, s.sz,
+                   a4, b4, c4);
+}
+
+// The closest-hit order as one 64-bit key: distance bits mapped to an
+// order-preserving unsigned (-0 folded onto +0, so equal distances compare
+// equal), then the global triangle index.  atomicMin over these keys picks
+// the hit of the sequential rule (smaller t, then smaller index) in any
+// order of arrival.
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t key) {
+    uint32_t b = __float_as_uint(__fadd_rn(t, 0.0f));
+    b ^= (uint32_t)((int32_t)b >> 31) | 0x80000000u;
+    return ((unsigned long long)b << 32) | key;
+}
+
+__device__ __forceinline__ float hit_key_t(unsigned long long k) {
+    uint32_t b = (uint32_t)(k >> 32);
+    b = (b & 0x80000000u) ? (b ^ 0x80000000u) : ~b;
+    return __uint_as_float(b);
+}
+
+// RayResult of a finished ray from its best hit key; the winning record's
+// edge functions are recomputed (same inputs as at acceptance, so the
+// same t and barycentrics).
+__device__ __forceinline__ void write_hit_key(int4* __restrict__ results, uint32_t ri, const RayS& s,
+                                              const float4* __restrict__ tris,
+                                              const uint32_t* __restrict__ rec_of_key, unsigned long long best) {
+    const uint32_t key = (uint32_t)best;
+    if (key == 0xFFFFFFFFu) {
+        write_miss(results, ri);
+        return;
+    }
+    const uint32_t rec = __ldg(&rec_of_key[key]);
+    float4 a4 = __ldg(&tris[3 * rec + 0]);
+    float4 b4 = __ldg(&tris[3 * rec + 1]);
+    float4 c4 = __ldg(&tris[3 * rec + 2]);
+    Uvw q = tri_uvw(s, a4, b4, c4);
+    float t = __fdiv_rn(q.T, q.det);
+    float u = __fdiv_rn(q.V, q.det), v = __fdiv_rn(q.W, q.det);
+    results[ri] = make_int4(__float_as_int(a4.w), __float_as_int(b4.w), __float_as_int(t), (int)pack_unorm2x16(u, v));
+}
+
+constexpr uint32_t kRecBits = 27;  // task word: lane << 27 | triangle record
+constexpr int kTaskCap = 32 * 24;  // a node hands a lane at most 24 triangles
+
+// Same traversal as k_trace_bvh8, except that triangle tests are shared by
+// the warp: after each node step every lane lists its (lane, triangle)
+// pairs in shared memory and the warp tests the list 32 pairs at a time,
+// each result folded into the owner's best hit key with a shared atomicMin.
+// Any-hit rays report the nearest hit of the first list that has one.
+template <bool CLOSEST, bool COUNT>
+__global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
+    const float4* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
+    int4* __restrict__ results, const uint32_t* __restrict__ ray_index, uint32_t n,
+    const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ rec_of_key, uint32_t* __restrict__ work,
+    uint32_t refill, uint32_t postpone) {
+    __shared__ RayS s_ray[kBlock];
+    __shared__ unsigned long long s_best[kBlock];
+    __shared__ uint32_t s_task[kBlock / 32][kTaskCap];
+    const uint32_t count = load_count(n, n_dev);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t wbase = threadIdx.x & ~31u;
+    uint32_t* const task = s_task[threadIdx.x >> 5];
+    uint2 stack[kStack8];
+    int sp = 0;
+    uint32_t ri = kNoRay;
+    enum : uint32_t { kIdle = 0, kTracing = 1, kDone = 2 };
+    uint32_t state = kIdle;
+    bool exhausted = false;
+    RayT r;
+    float tcur = 0.0f;
+    uint2 ng = make_uint2(0u, 0u);
+    uint32_t c_nodes = 0, c_tris = 0, c_rays = 0, c_iters = 0;
+    for (;;) {
+        bool want = state != kTracing && !exhausted;
+        uint32_t want_mask = __ballot_sync(0xffffffffu, want);
+        uint32_t busy_mask = __ballot_sync(0xffffffffu, state == kTracing);
+        if (want_mask != 0u && (__popc(want_mask) >= refill || busy_mask == 0u)) {
+            if (state == kDone) {
+                write_hit_key(results, ri, s_ray[threadIdx.x], tris, rec_of_key, s_best[threadIdx.x]);
+                state = kIdle;
+            }
+            uint32_t leader = __ffs(want_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&work[0], __popc(want_mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (want) {
+                uint32_t i = base + __popc(want_mask & lt_mask);
+                if (i < count) {
+                    uint32_t idx = ray_index ? ray_index[i] : i;
+                    float4 r0 = rays[2 * idx + 0];
+                    float4 r1 = rays[2 * idx + 1];
+                    if (!(r1.w >= r0.w)) {  // empty interval: miss, lane stays idle
+                        write_miss(results, idx);
+                    } else {
+                        ri = idx;
+                        state = kTracing;
+                        r = setup_ray(r0, r1);
+                        s_ray[threadIdx.x] = ray_shared(r);
+                        s_best[threadIdx.x] = hit_key(r1.w, 0xFFFFFFFFu);
+                        tcur = r1.w;
+                        sp = 0;
+                        ng = make_uint2(0u, 0x80000000u);
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        const uint32_t busy = __ballot_sync(0xffffffffu, state == kTracing);
+        if (__ballot_sync(0xffffffffu, state != kIdle || !exhausted) == 0u) break;
+        if (COUNT && lane == 0) ++c_iters;
+
+        uint32_t tri_base = 0, tg = 0;
+        if (state == kTracing) {
+            if (ng.y > 0x00FFFFFFu) {
+                uint32_t bit = 31u - __clz(ng.y);
+                ng.y &= ~(1u << bit);
+                uint32_t slot = (bit - 24u) ^ r.oct;
+                uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+                if (ng.y > 0x00FFFFFFu) {
+                    if (sp < kStack8) {
+                        stack[sp++] = ng;
+                    } else {
+                        raise_status(kErrBounds);
+                    }
+                }
+                uint32_t child_base, imask;
+                if (COUNT) ++c_nodes;
+                uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, tcur, child_base, tri_base, imask);
+                ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
+                tg = hitmask & 0x00FFFFFFu;
+            } else {
+                tri_base = ng.x;
+                tg = ng.y;
+                ng = make_uint2(0u, 0u);
+            }
+            if (postpone != 0u) {
+                uint32_t with_tris = __ballot_sync(busy, tg != 0u);
+                if (tg != 0u && ng.y > 0x00FFFFFFu && (uint32_t)__popc(with_tris) < postpone && sp < kStack8) {
+                    stack[sp++] = make_uint2(tri_base, tg);
+                    tg = 0;
+                }
+            }
+        }
+
+        // Warp-wide triangle list: exclusive scan of the per-lane counts.
+        const uint32_t cnt = __popc(tg);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total != 0u) {
+            uint32_t pos = incl - cnt;
+            const uint32_t owner = lane << kRecBits;
+            while (tg != 0u) {
+                uint32_t tb = __ffs(tg) - 1u;
+                tg &= tg - 1u;
+                task[pos++] = owner | (tri_base + tb);
+            }
+            __syncwarp();
+            for (uint32_t j = lane; j < total; j += 32u) {
+                const uint32_t w = task[j];
+                const uint32_t o = wbase + (w >> kRecBits);
+                const uint32_t rec = w & ((1u << kRecBits) - 1u);
+                const RayS rs = s_ray[o];
+                float4 a4 = __ldg(&tris[3 * rec + 0]);
+                float4 b4 = __ldg(&tris[3 * rec + 1]);
+                float4 c4 = __ldg(&tris[3 * rec + 2]);
+                Uvw q = tri_uvw(rs, a4, b4, c4);
+                if (q.edge_ok && q.det != 0.0f) {
+                    float t = __fdiv_rn(q.T, q.det);
+                    if (t >= rs.tmin) {
+                        // A stale read can only be larger than the current
+                        // best, so skipping on it is safe.
+                        unsigned long long hk = hit_key(t, __float_as_uint(c4.w));
+                        if (hk < s_best[o]) atomicMin(&s_best[o], hk);
+                    }
+                }
+            }
+            __syncwarp();
+            if (COUNT) c_tris += cnt;
+        }
+
+        if (state == kTracing) {
+            const unsigned long long best = s_best[threadIdx.x];
+            tcur = hit_key_t(best);
+            bool finished = false;
+            if (!CLOSEST && (uint32_t)best != 0xFFFFFFFFu) {
+                finished = true;
+            } else if (ng.y <= 0x00FFFFFFu) {
+                if (sp == 0) {
+                    finished = true;
+                } else {
+                    ng = stack[--sp];
+                }
+            }
+            if (finished) {
+                state = kDone;
+                if (COUNT) ++c_rays;
+            }
+        }
+    }
+    if (COUNT) add_counts(c_nodes, c_tris, c_rays, c_iters);
+    if (lane == 0) {
+        uint32_t warps = gridDim.x * (blockDim.x / 32);
+        __threadfence();
+        if (atomicAdd(&work[1], 1u) == warps - 1u) {
+            work[0] = 0u;
+            work[1] = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // Work-counter slots (16 u32 apart) handed out round robin, so concurrent
 // traces on different streams do not share a counter.
 static std::atomic<uint32_t> g_slot{0};
-static int g_blocks_per_sm[2] = {0, 0};
+// Resident blocks per SM: [closest] for the per-lane kernel, [2 + closest]
+// for the cooperative one.
+static int g_blocks_per_sm[4] = {0, 0, 0, 0};
 static int g_num_sms = 0;
 static uint32_t g_refill = 8;
 
 void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
 static uint32_t g_postpone = 0;
 void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
+static bool g_coop = true;
+void set_trace_coop(bool on) { g_coop = on; }
+bool get_trace_coop() { return g_coop; }
 uint32_t get_trace_refill() { return g_refill; }
 static bool g_count = false;
 void set_trace_count(bool on) { g_count = on; }
@@ -516,6 +769,12 @@ cudaError_t trace_prepare() {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[0], k_trace_bvh8<false, false>, kBlock, 0);
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[1], k_trace_bvh8<true, false>, kBlock, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[2], k_trace_bvh8_coop<false, false>, kBlock,
+                                                          0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_blocks_per_sm[3], k_trace_bvh8_coop<true, false>, kBlock,
+                                                          0);
     if (e == cudaSuccess) g_num_sms = sms;
     return e;
 }
@@ -545,14 +804,23 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             cudaError_t e = trace_prepare();
             if (e != cudaSuccess) return e;
         }
-        unsigned pgrid = (unsigned)(g_num_sms * (closest ? g_blocks_per_sm[1] : g_blocks_per_sm[0]));
+        // The cooperative kernel packs a triangle record into 27 bits.
+        const bool coop = g_coop && sc.bvh8_rec_of_key && sc.bvh8_num_tris < (1u << kRecBits);
+        unsigned pgrid = (unsigned)(g_num_sms * g_blocks_per_sm[(coop ? 2 : 0) + (closest ? 1 : 0)]);
         if (pgrid == 0) pgrid = 1;
         if (grid < pgrid) pgrid = grid;
         uint32_t* work = sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
-        auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
-                          : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);
-        k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, work, g_refill,
-                                    g_postpone);
+        if (coop) {
+            auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
+                              : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);
+            k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, sc.bvh8_rec_of_key,
+                                        work, g_refill, g_postpone);
+        } else {
+            auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
+                              : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);
+            k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, work, g_refill,
+                                        g_postpone);
+        }
     } else {
         auto k2 = closest ? (g_count ? k_trace_bvh2<true, true> : k_trace_bvh2<true, false>)
                           : (g_count ? k_trace_bvh2<false, true> : k_trace_bvh2<false, false>);

@@ -17,6 +17,9 @@ void set_trace_refill(uint32_t refill);
 void set_trace_postpone(uint32_t lanes);
 uint32_t get_trace_refill();
 uint32_t get_trace_postpone();
+// Warp-cooperative triangle tests in the BVH8 traversal (on by default).
+void set_trace_coop(bool on);
+bool get_trace_coop();
 // Counting variants of the traversal kernels (node visits, triangle tests,
 // rays, persistent-warp iterations) for diagnostics.
 void set_trace_count(bool on);
