@@ -217,6 +217,18 @@ def trace_bvh2(nodes: np.ndarray, tris: np.ndarray, rays, closest=True, ray_inde
     return res
 
 
+def trace_brute(tris: np.ndarray, rays, closest=True):
+    """Closest hit over every triangle record (no BVH), same test and tie
+    rule as trace_bvh2."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    t = np.ascontiguousarray(tris)
+    nt = t.nbytes // 48
+    res = np.empty((rays.shape[0], 4), np.int32)
+    _call(load().orc_trace_brute, ptr(t), C.c_uint32(nt), ptr(rays), ptr(res), C.c_uint32(rays.shape[0]),
+          C.c_int(1 if closest else 0))
+    return res
+
+
 class Fp64Scene:
     """FP64 closest/any-hit oracle over its own BVH."""
 

@@ -908,6 +908,30 @@ extern "C" void orc_fp64_trace(const void* scene, const ORay* rays, uint32_t n, 
     }
 }
 
+// Every triangle tested, no BVH: the closest hit (or the first hit in
+// record order for any-hit) under the same watertight test and tie rule.
+// Checks that box culling in the traversal above is conservative.
+extern "C" void orc_trace_brute(const void* tris, uint32_t num_tris, const ORay* rays, OHit* results, uint32_t n,
+                                int closest) {
+    const TriRec* T = (const TriRec*)tris;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < (long long)n; ++i) {
+        const ORay& ray = rays[i];
+        OHit& out = results[i];
+        out = OHit{-1, -1, -1.0f, 0};
+        if (!(ray.tmax >= ray.tmin)) continue;
+        RaySetup r = setup(ray);
+        Best h{ray.tmax, 0xFFFFFFFFu, -1, -1, 0, 0};
+        bool found = false;
+        for (uint32_t k = 0; k < num_tris; ++k)
+            if (tri_test(r, T[k], h)) {
+                found = true;
+                if (!closest) break;
+            }
+        if (found) out = OHit{h.prim, h.geom, h.t, pack_unorm(h.u, h.v)};
+    }
+}
+
 // ---------------------------------------------------------- whole frame
 // Renderer::render with rayType path (Renderer.cpp:552-654, :175-199): the
 // CPU pipeline over the same scene, BVH2 and geometry, used for end-to-end

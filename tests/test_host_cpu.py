@@ -220,6 +220,40 @@ def test_cpu_traversal_agrees_with_fp64(wf, orc):
     assert np.array_equal(anyr[:, 0] >= 0, hit)
 
 
+def adversarial_rays(rng, pos, idx, n):
+    """Rays that start on triangles (tmin 0), half of them on an edge, and
+    rays aimed at edges and vertices from in front of the surface."""
+    tri = rng.integers(0, idx.shape[0], n)
+    v = pos[idx[tri]]
+    w = rng.dirichlet((1, 1, 1), n).astype(np.float32)
+    w[: n // 4, 2] = 0.0
+    w[n // 8: n // 4, 1] = 0.0  # a vertex
+    w /= np.maximum(w.sum(1, keepdims=True), 1e-30)
+    p = np.einsum("nk,nkd->nd", w, v).astype(np.float32)
+    rays = random_rays(rng, n, tmax=1e30)
+    rays[:, :3] = p
+    rays[n // 2:, :3] -= 2.0 * rays[n // 2:, 4:7]
+    return rays
+
+
+@pytest.mark.parametrize("scene", [(0, 9, 3000), (1, 1, 0)])
+def test_bvh2_culling_is_conservative(wf, orc, scene):
+    """The oracle's BVH2 traversal over the product's BVH (boxes grown by
+    the build margin) returns the brute-force closest hit on rays that start
+    on surfaces or hit edges and vertices, where culling with exact-fit boxes
+    drops tied triangles."""
+    kind, seed, ntris = scene
+    pos, _, idx = wf.api.generate_scene(kind, seed, ntris)
+    sc = wf.api.Scene(pos, idx, host_only=True)
+    nodes, tris = sc.export_bvh2()
+    rng = np.random.default_rng(31)
+    n = 3000 if kind == 0 else 300
+    rays = adversarial_rays(rng, pos, idx, n)
+    a = orc.trace_bvh2(nodes, tris, rays)
+    b = orc.trace_brute(tris, rays)
+    assert np.array_equal(a, b)
+
+
 def test_cpu_frame_runs(wf, orc):
     pos, nrm, idx = wf.api.generate_scene(0, 3, 4000)
     sc = wf.api.Scene(pos, idx, host_only=True)

@@ -253,6 +253,30 @@ void build_bvh2(const BuildInput& in, int max_leaf, HostBvh2& out) {
         out.depth = 1;
         return;
     }
+    // Stored boxes are the triangle bounds grown by delta = 2^-22 * P on
+    // every side, P = the largest absolute vertex coordinate.  With
+    // u = 2^-24, the traversal's slab distances fma(p, inv, -o*inv) are off
+    // by at most about u * (|o| + P) * |inv|, which delta * |inv| = 4 u * P *
+    // |inv| covers while |o| <= 3 P; from |o| >= 2 P on that error is within
+    // 2 u of t itself and inside the relative slack on exit distances.  The
+    // rounding of a triangle's own t near the ray origin (a few u times the
+    // triangle's size) is covered as well for triangles up to about P / 2
+    // across.  So culling does not drop a triangle that ties the current
+    // closest hit, including hits at t = 0 of rays that start on a surface:
+    // checked against a brute-force oracle on such rays.  (Each doubling of
+    // delta costs about 1% of frame throughput: shadow rays start 1e-5
+    // before their surface and enter its grown box.)
+    float P = 0.0f;
+    for (const Prim& p : prims)
+        for (int k = 0; k < 3; ++k) P = std::max(P, std::max(std::fabs(p.box.lo[k]), std::fabs(p.box.hi[k])));
+    const float delta = P * 0x1p-22f;
+    auto grown = [delta](Box b) {
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] -= delta;
+            b.hi[k] += delta;
+        }
+        return b;
+    };
     std::vector<uint32_t> idx(N);
     for (uint32_t i = 0; i < N; ++i) idx[i] = i;
     Builder B(prims, idx, max_leaf);
@@ -273,7 +297,7 @@ void build_bvh2(const BuildInput& in, int max_leaf, HostBvh2& out) {
     std::vector<Item> stack;
     if (B.nodes[root].count > 0) {
         Bvh2Node r = empty_node;
-        set_child(r, 0, B.nodes[root].box, emit_leaf(B.nodes[root]));
+        set_child(r, 0, grown(B.nodes[root].box), emit_leaf(B.nodes[root]));
         set_child(r, 1, none, r.link[0]);
         out.nodes.push_back(r);
         return;
@@ -295,7 +319,7 @@ void build_bvh2(const BuildInput& in, int max_leaf, HostBvh2& out) {
                 out.nodes.push_back(empty_node);
                 stack.push_back({(uint32_t)ch[c], (uint32_t)link});
             }
-            set_child(out.nodes[it.slot], c, cn.box, link);
+            set_child(out.nodes[it.slot], c, grown(cn.box), link);
         }
     }
 }
