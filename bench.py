@@ -52,6 +52,12 @@ PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, s
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
+# DRAM bytes (read + write) per ray of the BVH8 traversal launches, from one
+# ncu capture of the 960x540 bounce-1 case (dram__bytes_read.sum +
+# dram__bytes_write.sum over the launch's rays); the traffic of a launch
+# grows with its ray count, so a full launch's traffic is this times its
+# rays.  None until captured.
+TRACE_DRAM_BYTES_PER_RAY = {"any": None, "closest": None}
 
 
 def peaks():
@@ -205,11 +211,18 @@ def run_ours(args):
     out = None
     if rank == 0:
         cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
-        tr = micro["trace_chosen"]
-        roof = {"kernel": "k_trace_bvh8 (closest hit, bounce-1 path rays after sort+reorder)", "bound": "hbm",
-                "achieved": tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                "frac": tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9 / hbm, "traffic": None,
-                "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_ray": 48}
+        def trace_roof(tr, kernel, kind):
+            ach = tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9
+            per_ray = TRACE_DRAM_BYTES_PER_RAY[kind]
+            return {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                    "frac": ach / hbm, "traffic": None if per_ray is None else per_ray * tr["rays"],
+                    "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_ray": 48,
+                    "launch_ms": tr["ms"], "rays_per_launch": tr["rays"]}
+
+        roof = trace_roof(micro["trace_shadow"], "k_trace_bvh8_coop<any-hit> (bounce-1 shadow rays, 2 per path ray)",
+                          "any")
+        closest_roof = trace_roof(micro["trace_chosen"],
+                                  "k_trace_bvh8_coop<closest> (bounce-1 path rays after sort+reorder)", "closest")
         srt = micro["sort"]
         sort_roof = {"kernel": "radix sort u64 keys (63 bits, 8 passes) + u32 values", "bound": "hbm",
                      "achieved": srt["gbs"], "peak": hbm, "unit": "GB/s", "frac": srt["gbs"] / hbm,
@@ -230,7 +243,7 @@ def run_ours(args):
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),
                              "reorder_frac": round(micro["reorder"]["gbs"] / hbm, 3)},
-            "roofline": roof, "sort_roofline": sort_roof,
+            "roofline": roof, "closest_roofline": closest_roof, "sort_roofline": sort_roof,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 36,
                     "d2h_bytes_per_step": w * h * 16,
@@ -307,6 +320,17 @@ def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
     api.reorder(ids, path, out, s2i, os2i, oi2s)
     ms_trace8 = timeit(lambda: api.trace(scene, wf.BVH8_Q8, out, res))
     ms_trace2_sorted = timeit(lambda: api.trace(scene, wf.BVH2_FP32, out, res))
+    # The bounce's shadow rays (2 per path ray, toward the area light): the
+    # any-hit traversal that takes the largest share of a frame.
+    S = COURTYARD["renderer"]["num_shadow_samples"]
+    srays = torch.empty((S * m, 8), dtype=torch.float32, device=dev)
+    ss2i = torch.empty(S * m, dtype=torch.int32, device=dev)
+    si2s = torch.empty(S * m, dtype=torch.int32, device=dev)
+    sres = torch.empty((S * m, 4), dtype=torch.int32, device=dev)
+    api.raygen_shadow(seeds, out, res, srays, ss2i, si2s, COURTYARD["light"], COURTYARD["renderer"]["shadow_radius"],
+                      0, m, S)
+    ms_shadow8 = timeit(lambda: api.trace(scene, wf.BVH8_Q8, srays, sres, closest_hit=False))
+    ms_shadow2 = timeit(lambda: api.trace(scene, wf.BVH2_FP32, srays, sres, closest_hit=False))
     ms_sort = timeit(lambda: api.sort_pairs(keys, ids, 63, scratch=scratch))
     ms_morton = timeit(lambda: api.morton(path, smin, ssize, wf.MORTON_6D64, keys, ids))
     ms_reorder = timeit(lambda: api.reorder(ids, path, out, s2i, os2i, oi2s))
@@ -319,8 +343,11 @@ def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
                        "chosen_over_plain_composite": round(ms_plain / ms_comp, 3),
                        "chosen_over_plain_trace_only": round(ms_plain / ms_trace8, 3),
                        "morton_ms": round(ms_morton, 4), "sort_ms": round(ms_sort, 4),
-                       "reorder_ms": round(ms_reorder, 4)},
-        "trace_chosen": {"ms": ms_trace8, "alg_bytes": 48.0 * m},
+                       "reorder_ms": round(ms_reorder, 4),
+                       "shadow_rays": S * m, "shadow_bvh8_mrays_s": round(S * m / (ms_shadow8 * 1e-3) / 1e6, 2),
+                       "shadow_bvh2_mrays_s": round(S * m / (ms_shadow2 * 1e-3) / 1e6, 2)},
+        "trace_chosen": {"ms": ms_trace8, "alg_bytes": 48.0 * m, "rays": m},
+        "trace_shadow": {"ms": ms_shadow8, "alg_bytes": 48.0 * S * m, "rays": S * m},
         "sort": {"n": m, "ms": ms_sort, "gbs": 192.0 * m / (ms_sort * 1e-3) / 1e9},
         "reorder": {"n": m, "ms": ms_reorder, "gbs": 80.0 * m / (ms_reorder * 1e-3) / 1e9},
     }
@@ -430,11 +457,11 @@ def cpu_frame(args, api, scene, pos, nrm, idx, w, h, form):
 
 def cpu_baseline(args, wf, api, scene, pos, nrm, idx):
     import oracle
-    w, h = 480, 270
+    w, h = COURTYARD["width"], COURTYARD["height"]
     rays, dt = cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
     return {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"one {w}x{h} frame of the courtyard workload (1/16 of the pixels), chosen-form settings, "
-                      f"CPU oracle with FP32 BVH2 traversal; {int(rays)} rays in {dt:.2f} s"}
+            "sample": f"one full {w}x{h} frame of the courtyard workload, chosen-form settings, CPU oracle with "
+                      f"FP32 BVH2 traversal; {int(rays)} rays in {dt:.2f} s"}
 
 
 # ---------------------------------------------------------- reference arm
@@ -450,7 +477,7 @@ def run_reference(args):
     W = COURTYARD
     pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
     scene = api.Scene(pos, idx, host_only=True)
-    w, h = 480, 270
+    w, h = 960, 540  # a quarter of the pixels per step keeps --steps 50 within a few minutes
     for _ in range(args.warmup):
         cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
     total_rays, total_t = 0, 0.0
@@ -465,7 +492,7 @@ def run_reference(args):
            "data": "synthetic (seeded scene)", "config": {"workload": WORKLOAD_NAME},
            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": oracle.num_threads(),
                             "kind": "port",
-                            "sample": f"each step one {w}x{h} frame of the courtyard workload (1/16 of the "
+                            "sample": f"each step one {w}x{h} frame of the courtyard workload (1/4 of the "
                                       "pixels) on the CPU restatement of the reference shaders (the reference's "
                                       "Vulkan/rayQuery path is unavailable on this box)"},
            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

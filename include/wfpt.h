@@ -128,6 +128,8 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          0 = each lane tests its own.  Closest hits are
  *                          identical; an any-hit ray may report a different
  *                          (equally valid) occluder
+ *   "sort.tiles"           radix sort tile size: 0 = by problem size
+ *                          (default), 1 = small tiles, 2 = large tiles
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */

@@ -119,3 +119,26 @@ def test_sort_scratch_too_small(wf, dev):
     small = torch.empty(64, dtype=torch.uint8, device=dev)
     with pytest.raises(wf.WfptError):
         wf.api.sort_pairs(k, v, 32, scratch=small)
+
+
+@pytest.mark.parametrize("tiles", [1, 2])
+@pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4097, 32), (123457, 32),
+                                        (1535, 63), (1537, 64), (3073, 63), (300001, 48), (2073600, 63)])
+def test_sort_tile_variants(wf, dev, tiles, n, key_bits):
+    """Both tile sizes give the stable order, at sizes around both tile
+    boundaries, including the frame's wavefront size."""
+    rng = np.random.default_rng(n + key_bits)
+    if key_bits > 32:
+        keys = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
+    else:
+        keys = rng.integers(0, 2**32, n, dtype=np.uint32)
+    keys[::5] = keys[len(keys) // 2]  # duplicates: stability matters
+    old = wf.api.tune_get("sort.tiles")
+    try:
+        wf.api.tune_set("sort.tiles", tiles)
+        k, v = run_sort(wf, dev, keys, key_bits)
+    finally:
+        wf.api.tune_set("sort.tiles", old)
+    rk, rv = stable_ref(keys, key_bits)
+    assert np.array_equal(v, rv) and np.array_equal(k, rk)
+    assert wf.api.device_status() == 0

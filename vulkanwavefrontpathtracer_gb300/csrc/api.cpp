@@ -101,6 +101,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_trace_coop(value != 0);
         return WFPT_OK;
     }
+    if (k == "sort.tiles") {
+        if (value < 0 || value > 2) return invalid("sort.tiles must be 0 (auto), 1 (small) or 2 (large)");
+        wfpt::set_sort_tiles((int)value);
+        return WFPT_OK;
+    }
     if (k == "trace.count") {
         if (value < 0 || value > 1) return invalid("trace.count must be 0 or 1");
         wfpt::set_trace_count(value != 0);
@@ -129,6 +134,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "trace.bvh8.coop") {
         *value = wfpt::get_trace_coop() ? 1 : 0;
+        return WFPT_OK;
+    }
+    if (k == "sort.tiles") {
+        *value = wfpt::get_sort_tiles();
         return WFPT_OK;
     }
     if (k == "trace.count") {

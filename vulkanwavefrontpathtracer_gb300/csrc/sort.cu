@@ -2,15 +2,20 @@
 //
 // Replaces the reference's vrdxCmdSortKeyValue (upsweep -> spine ->
 // downsweep per pass, external/vulkan_radix_sort/vk_radix_sort.h:2598-2755)
-// with the single-sweep scheme of Adinets & Merrill ("Onesweep", 2022):
+// with a single-sweep scheme after Adinets & Merrill ("Onesweep", 2022):
 //   1. one histogram kernel reads the keys once and builds the 256-bin digit
-//      histogram of every pass;
-//   2. per pass, one kernel: each 256-thread CTA takes the next tile from a
-//      ticket counter, ranks its keys with warp ballots (stable: keys are
-//      ranked in input order), publishes its per-digit counts, resolves the
+//      histogram of every pass (the global digit bases);
+//   2. per pass, one kernel of 1024-thread CTAs, one CTA per SM: each takes
+//      the next tile from a ticket counter, ranks its keys with warp ballots
+//      (stable: keys are ranked in input order), publishes its per-digit
+//      counts, stages the tile in shared memory in digit order, resolves the
 //      global digit offsets with a bounded decoupled look-back over earlier
-//      tiles, stages the tile in shared memory in digit order and writes
-//      keys and values out in coalesced runs.
+//      tiles and writes keys and values out in coalesced runs.
+// Sized for a frame's wavefronts (a few million keys, all of it resident in
+// L2): tiles of 8 or 14-16 keys per thread make such a pass one wave of
+// about one tile per SM, and the look-back reads 16 predecessors per L2 round
+// trip, so the prefix crosses a wave in a handful of round trips; staging
+// the tile before the look-back overlaps that wait with useful work.
 // Ping-pong between the caller's buffers and scratch; after an even number
 // of passes the result is back in the caller's buffers (as in the reference),
 // after an odd number it is copied back.
@@ -24,28 +29,18 @@ namespace wfpt {
 
 cudaError_t status_sort(uint32_t* out) { return read_and_clear_status(out); }
 
-constexpr int kSortBlock = 256;  // one thread per digit value
+constexpr int kSortThreads = 1024;
+constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kRadix = 256;
-constexpr int kSortWarps = kSortBlock / 32;
+constexpr int kHistBlock = 256;
 constexpr uint32_t kLbAggregate = 1u << 30;
 constexpr uint32_t kLbPrefix = 2u << 30;
 constexpr uint32_t kLbValue = (1u << 30) - 1u;
+constexpr int kLbChunk = 16;  // predecessors read per look-back round trip
 
-template <typename K>
-struct SortCfg;
-template <>
-struct SortCfg<uint32_t> {
-    static constexpr int kKpt = 16;
-};
-template <>
-struct SortCfg<uint64_t> {
-    static constexpr int kKpt = 12;
-};
-
-template <typename K>
-constexpr int tile_of() {
-    return kSortBlock * SortCfg<K>::kKpt;
-}
+// Keys per thread of the two tile variants (tile = 1024 * KPT keys).
+constexpr int kKptSmall32 = 8, kKptLarge32 = 16;
+constexpr int kKptSmall64 = 8, kKptLarge64 = 14;
 
 // Digit mask of pass p: the top pass keeps only the bits below key_bits.
 __host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p) {
@@ -55,8 +50,10 @@ __host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p) {
 __device__ __forceinline__ uint32_t digit_of(uint32_t k, int shift, uint32_t dmask) { return (k >> shift) & dmask; }
 __device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift, uint32_t dmask) { return (uint32_t)(k >> shift) & dmask; }
 
-// Exclusive scan of one value per thread over a 256-thread block.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp) {
+// Exclusive scan of one value per thread over the whole block (blockDim.x =
+// 32 * W); *total receives the block sum.  Every thread must call it.
+template <int W>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
     uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t x = v;
 #pragma unroll
@@ -66,46 +63,92 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
     }
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    uint32_t off = 0;
+    uint32_t off = 0, sum = 0;
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w)
-        if (w < (int)warp) off += s_warp[w];
+    for (int w = 0; w < W; ++w) {
+        uint32_t c = s_warp[w];
+        if (w < (int)warp) off += c;
+        sum += c;
+    }
     __syncthreads();
+    *total = sum;
     return off + x - v;
 }
 
-// Histogram of every pass's digit over the first `count` keys.
-template <typename K>
-__global__ void __launch_bounds__(kSortBlock) k_sort_hist(const K* __restrict__ keys, uint32_t n,
-                                                           const uint32_t* __restrict__ n_dev, int passes,
-                                                           int key_bits, uint32_t* __restrict__ hist) {
-    __shared__ uint32_t s_h[8 * kRadix];
-    for (int i = threadIdx.x; i < passes * kRadix; i += kSortBlock) s_h[i] = 0;
+// Byte p of a key (digit of pass p before the top-pass mask).
+__device__ __forceinline__ uint32_t key_byte(uint32_t k, int p) { return p < 4 ? (k >> (8 * p)) & 0xFFu : 0u; }
+__device__ __forceinline__ uint32_t key_byte(uint64_t k, int p) {
+    return p < 4 ? ((uint32_t)k >> (8 * p)) & 0xFFu : ((uint32_t)(k >> 32) >> (8 * (p - 4))) & 0xFFu;
+}
+
+// Histogram of every pass's digit over the first `count` keys: PASSES is a
+// template parameter so that the digit extraction unrolls into constant
+// byte selects; each thread issues the loads of 8 keys before their
+// shared-memory atomics.
+template <typename K, int PASSES>
+__global__ void __launch_bounds__(kHistBlock) k_sort_hist(const K* __restrict__ keys, uint32_t n,
+                                                           const uint32_t* __restrict__ n_dev, uint32_t top_mask,
+                                                           uint32_t* __restrict__ hist) {
+    constexpr int U = 8;
+    __shared__ uint32_t s_h[PASSES * kRadix];
+    for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistBlock) s_h[i] = 0;
     __syncthreads();
-    uint32_t count = load_count(n, n_dev);
-    for (uint32_t i = blockIdx.x * kSortBlock + threadIdx.x; i < count; i += gridDim.x * kSortBlock) {
-        K k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p * kRadix + digit_of(k, 8 * p, pass_mask(key_bits, p))], 1u);
+    const uint32_t count = load_count(n, n_dev);
+    const uint32_t step = gridDim.x * kHistBlock * U;
+    for (uint32_t i0 = blockIdx.x * kHistBlock * U + threadIdx.x; i0 < count; i0 += step) {
+        K kk[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint32_t i = i0 + u * kHistBlock;
+            kk[u] = i < count ? keys[i] : (K)0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (i0 + u * kHistBlock < count) {
+#pragma unroll
+                for (int p = 0; p < PASSES; ++p) {
+                    uint32_t d = key_byte(kk[u], p);
+                    if (p == PASSES - 1) d &= top_mask;
+                    atomicAdd(&s_h[p * kRadix + d], 1u);
+                }
+            }
+        }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * kRadix; i += kSortBlock) {
+    for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistBlock) {
         uint32_t c = s_h[i];
         if (c) atomicAdd(&hist[i], c);
     }
 }
 
-// One digit pass.  Dynamic shared memory: TILE keys, TILE values,
-// kSortWarps*256 per-warp digit counters, 256 global bases, 256 local offsets.
 template <typename K>
-__global__ void __launch_bounds__(kSortBlock, 4) k_onesweep(const K* __restrict__ keys_in,
-                                                          const uint32_t* __restrict__ vals_in,
-                                                          K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                          uint32_t n, const uint32_t* __restrict__ n_dev, int shift, uint32_t dmask,
-                                                          const uint32_t* __restrict__ hist,
-                                                          uint32_t* __restrict__ lookback,
-                                                          uint32_t* __restrict__ ticket) {
-    constexpr int KPT = SortCfg<K>::kKpt;
-    constexpr int TILE = kSortBlock * KPT;
+static void launch_hist(const K* keys, uint32_t n, const uint32_t* n_dev, int passes, int key_bits,
+                        uint32_t* hist, unsigned grid, cudaStream_t s) {
+    const uint32_t top = pass_mask(key_bits, passes - 1);
+    switch (passes) {
+#define WFPT_HIST(P)                                                                                   \
+    case P:                                                                                            \
+        k_sort_hist<K, P><<<grid, kHistBlock, 0, s>>>(keys, n, n_dev, top, hist);                      \
+        break;
+        WFPT_HIST(1) WFPT_HIST(2) WFPT_HIST(3) WFPT_HIST(4) WFPT_HIST(5) WFPT_HIST(6) WFPT_HIST(7) WFPT_HIST(8)
+#undef WFPT_HIST
+        default: break;
+    }
+}
+
+// One digit pass.  Dynamic shared memory: TILE keys, TILE values,
+// kSortWarps*256 per-warp digit counters, 256 global bases, 256 local
+// offsets.
+template <typename K, int KPT>
+__global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              K* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, uint32_t n,
+                                                              const uint32_t* __restrict__ n_dev, int shift,
+                                                              uint32_t dmask, const uint32_t* __restrict__ hist,
+                                                              uint32_t* __restrict__ lookback,
+                                                              uint32_t* __restrict__ ticket) {
+    constexpr uint32_t TILE = kSortThreads * KPT;
     extern __shared__ __align__(16) unsigned char smem[];
     K* s_keys = reinterpret_cast<K*>(smem);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
@@ -118,7 +161,7 @@ __global__ void __launch_bounds__(kSortBlock, 4) k_onesweep(const K* __restrict_
     const uint32_t count = load_count(n, n_dev);
     const uint32_t ntiles = (count + TILE - 1) / TILE;
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortBlock) s_hist[i] = 0;
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
     if (tile >= ntiles) return;
@@ -156,62 +199,33 @@ __global__ void __launch_bounds__(kSortBlock, 4) k_onesweep(const K* __restrict_
     }
     __syncthreads();
 
-    // Thread t owns digit t: warp-exclusive prefixes and the tile count.
-    const uint32_t d = threadIdx.x;
+    // Threads 0..255 own one digit each: warp-exclusive prefixes and the
+    // tile's count of that digit.
+    const bool owner = threadIdx.x < kRadix;
+    const uint32_t d = threadIdx.x & (kRadix - 1);
     uint32_t run = 0;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-        uint32_t c = s_hist[w * kRadix + d];
-        s_hist[w * kRadix + d] = run;
-        run += c;
-    }
-    // Decoupled look-back for digit d.
-    uint32_t* lb = lookback + (size_t)tile * kRadix + d;
-    uint32_t excl;
-    if (tile == 0) {
-        // Global exclusive digit offset from the histogram.
-        excl = block_exclusive_scan(hist[d], s_scan);
-        atomicExch(lb, kLbPrefix | (excl + run));
-    } else {
-        atomicExch(lb, kLbAggregate | run);
-        excl = 0;
-        // Walk back over predecessors, reading kChunk of them with
-        // independent loads per round trip; stop at the first inclusive
-        // prefix, wait (bounded) on an entry that is not published yet.
-        constexpr int kChunk = 8;
-        int32_t j = (int32_t)tile - 1;
-        uint32_t spins = 0;
-        bool done = false;
-        while (!done && j >= 0) {
-            uint32_t st[kChunk];
-#pragma unroll
-            for (int q = 0; q < kChunk; ++q)
-                st[q] = (j - q >= 0) ? *((volatile uint32_t*)(lookback + (size_t)(j - q) * kRadix + d))
-                                     : uint32_t(kLbPrefix);
-            int used = 0;
-#pragma unroll
-            for (int q = 0; q < kChunk; ++q) {
-                if (done || used < q) continue;  // stopped earlier in this chunk
-                uint32_t flag = st[q] & ~kLbValue;
-                if (flag == 0u) continue;  // not published: re-read from here
-                excl += st[q] & kLbValue;
-                used = q + 1;
-                if (flag == kLbPrefix) done = true;
-            }
-            j -= used;
-            if (!done && used < kChunk && j >= 0) {
-                if (++spins > kSpinLimit) {
-                    raise_status(kErrTimeout);
-                    break;
-                }
-                __nanosleep(32);
-            }
+    if (owner) {
+#pragma unroll 8
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = s_hist[w * kRadix + d];
+            s_hist[w * kRadix + d] = run;
+            run += c;
         }
-        atomicExch(lb, kLbPrefix | (excl + run));
     }
-    uint32_t loc = block_exclusive_scan(run, s_scan);
-    s_loc[d] = loc;
-    s_base[d] = excl - loc;
+    uint32_t tile_total;
+    const uint32_t loc = block_exclusive_scan<kSortWarps>(owner ? run : 0u, s_scan, &tile_total);
+    // Publish this tile's counts (tile 0: its inclusive prefix, from the
+    // global histogram) before staging, so that successors can proceed.
+    uint32_t excl = 0;
+    if (tile == 0) {
+        uint32_t total;
+        excl = block_exclusive_scan<kSortWarps>(owner ? hist[d] : 0u, s_scan, &total);
+    }
+    uint32_t* lb = lookback + (size_t)tile * kRadix + d;
+    if (owner) {
+        s_loc[d] = loc;
+        atomicExch(lb, tile == 0 ? (kLbPrefix | (excl + run)) : (kLbAggregate | run));
+    }
     __syncthreads();
 
     // Stage the tile in digit order; values are read here, straight from
@@ -226,9 +240,46 @@ __global__ void __launch_bounds__(kSortBlock, 4) k_onesweep(const K* __restrict_
             s_vals[pos] = vals_in[i];
         }
     }
+
+    // Decoupled look-back for digit d: walk back over predecessors, kLbChunk
+    // of them per round trip with independent loads; stop at the first
+    // inclusive prefix, wait (bounded) on an entry that is not published yet.
+    if (owner && tile != 0) {
+        int32_t j = (int32_t)tile - 1;
+        uint32_t spins = 0;
+        bool done = false;
+        while (!done && j >= 0) {
+            uint32_t st[kLbChunk];
+#pragma unroll
+            for (int q = 0; q < kLbChunk; ++q)
+                st[q] = (j - q >= 0) ? *((volatile uint32_t*)(lookback + (size_t)(j - q) * kRadix + d))
+                                     : uint32_t(kLbPrefix);
+            int used = 0;
+#pragma unroll
+            for (int q = 0; q < kLbChunk; ++q) {
+                if (done || used < q) continue;  // stopped earlier in this chunk
+                uint32_t flag = st[q] & ~kLbValue;
+                if (flag == 0u) continue;  // not published: re-read from here
+                excl += st[q] & kLbValue;
+                used = q + 1;
+                if (flag == kLbPrefix) done = true;
+            }
+            j -= used;
+            if (!done && used < kLbChunk && j >= 0) {
+                if (++spins > kSpinLimit) {
+                    raise_status(kErrTimeout);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        atomicExch(lb, kLbPrefix | (excl + run));
+    }
+    if (owner) s_base[d] = excl - loc;
     __syncthreads();
-    const uint32_t tile_count = min((uint32_t)TILE, count - tile * TILE);
-    for (uint32_t j = threadIdx.x; j < tile_count; j += kSortBlock) {
+
+    const uint32_t tile_count = min(TILE, count - tile * TILE);
+    for (uint32_t j = threadIdx.x; j < tile_count; j += kSortThreads) {
         K kk = s_keys[j];
         uint32_t g = s_base[digit_of(kk, shift, dmask)] + j;
         if (g < count) {  // only fails after a look-back timeout
@@ -254,30 +305,55 @@ __global__ void k_copy_back(const K* __restrict__ ks, const uint32_t* __restrict
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-template <typename K>
+template <typename K, int KPT>
 static size_t onesweep_smem() {
-    constexpr int TILE = tile_of<K>();
-    return (size_t)TILE * sizeof(K) + (size_t)TILE * 4 + (size_t)(kSortWarps + 2) * kRadix * 4;
+    return (size_t)kSortThreads * KPT * (sizeof(K) + 4) + (size_t)(kSortWarps + 2) * kRadix * 4;
 }
 
-// Opts the pass kernels into their dynamic shared memory once (not a stream
-// operation, so the renderer calls it before capturing a frame graph).
+static int g_num_sms = 0;
+
+// Opts the pass kernels into their dynamic shared memory and reads the SM
+// count once (host calls that must not run inside a stream capture; the
+// renderer calls this before capturing a frame graph).
 cudaError_t sort_prepare() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_onesweep<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)onesweep_smem<uint32_t>());
+    if (g_num_sms != 0) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_onesweep<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)onesweep_smem<uint64_t>());
-    if (e == cudaSuccess) done = true;
+        e = cudaFuncSetAttribute(k_onesweep<uint32_t, kKptSmall32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)onesweep_smem<uint32_t, kKptSmall32>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_onesweep<uint32_t, kKptLarge32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)onesweep_smem<uint32_t, kKptLarge32>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_onesweep<uint64_t, kKptSmall64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)onesweep_smem<uint64_t, kKptSmall64>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_onesweep<uint64_t, kKptLarge64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)onesweep_smem<uint64_t, kKptLarge64>());
+    int dev = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) g_num_sms = sms > 0 ? sms : 1;
     return e;
+}
+
+// Tile variant: 0 = automatic, 1 = small tiles, 2 = large tiles.  Automatic
+// takes the small tiles while they fit in one wave (one tile per SM) and the
+// large ones otherwise, which halves the waves of a frame-sized sort.
+static int g_sort_tiles = 0;
+void set_sort_tiles(int v) { g_sort_tiles = v < 0 ? 0 : (v > 2 ? 2 : v); }
+int get_sort_tiles() { return g_sort_tiles; }
+
+static bool use_large_tiles(uint32_t n, bool wide) {
+    if (g_sort_tiles != 0) return g_sort_tiles == 2;
+    const size_t small = (size_t)kSortThreads * (wide ? kKptSmall64 : kKptSmall32);
+    return ((size_t)n + small - 1) / small > (size_t)g_num_sms;
 }
 
 struct SortLayout {
     int passes;
     size_t key_bytes;
-    size_t tiles;
+    size_t tiles;  // tiles of the small variant (the larger count)
     size_t off_ticket, off_hist, off_lookback, off_keys, off_vals, total;
 };
 
@@ -285,8 +361,8 @@ static SortLayout sort_layout(uint32_t max_n, int key_bits) {
     SortLayout L;
     L.passes = (key_bits + 7) / 8;
     L.key_bytes = key_bits <= 32 ? 4 : 8;
-    size_t tile = key_bits <= 32 ? tile_of<uint32_t>() : tile_of<uint64_t>();
-    L.tiles = ((size_t)max_n + tile - 1) / tile;
+    size_t tile = (size_t)kSortThreads * (key_bits <= 32 ? kKptSmall32 : kKptSmall64);
+    L.tiles = std::max<size_t>(1, ((size_t)max_n + tile - 1) / tile);
     L.off_ticket = 0;
     L.off_hist = 256;
     L.off_lookback = L.off_hist + align256((size_t)L.passes * kRadix * 4);
@@ -301,51 +377,59 @@ size_t sort_scratch_bytes(uint32_t max_n, int key_bits) {
     return sort_layout(max_n, key_bits).total;
 }
 
-template <typename K>
-static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
-                             unsigned char* scratch, cudaStream_t s) {
-    SortLayout L = sort_layout(n, key_bits);
-    // Tickets, histograms and look-back states start at zero.
-    cudaError_t e = cudaMemsetAsync(scratch, 0, L.off_keys, s);
-    if (e != cudaSuccess) return e;
+template <typename K, int KPT>
+static cudaError_t sort_passes(K* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
+                               const SortLayout& L, unsigned char* scratch, cudaStream_t s) {
+    constexpr uint32_t TILE = kSortThreads * KPT;
     uint32_t* tickets = reinterpret_cast<uint32_t*>(scratch + L.off_ticket);
     uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.off_hist);
     uint32_t* lookback = reinterpret_cast<uint32_t*>(scratch + L.off_lookback);
     K* alt_keys = reinterpret_cast<K*>(scratch + L.off_keys);
     uint32_t* alt_vals = reinterpret_cast<uint32_t*>(scratch + L.off_vals);
-
-    unsigned hgrid = (unsigned)std::min<size_t>(((size_t)n + kSortBlock * 8 - 1) / (kSortBlock * 8), 152 * 4);
-    if (hgrid == 0) hgrid = 1;
-    k_sort_hist<K><<<hgrid, kSortBlock, 0, s>>>(keys, n, n_dev, L.passes, key_bits, hist);
-    count_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-
-    size_t smem = onesweep_smem<K>();
-    if ((e = sort_prepare()) != cudaSuccess) return e;
+    const uint32_t tiles = (n + TILE - 1) / TILE;
+    const size_t smem = onesweep_smem<K, KPT>();
+    cudaError_t e;
     K* src_k = keys;
     uint32_t* src_v = values;
     K* dst_k = alt_keys;
     uint32_t* dst_v = alt_vals;
-    unsigned grid = (unsigned)(L.tiles == 0 ? 1 : L.tiles);
     for (int p = 0; p < L.passes; ++p) {
-        k_onesweep<K><<<grid, kSortBlock, smem, s>>>(src_k, src_v, dst_k, dst_v, n, n_dev, 8 * p, pass_mask(key_bits, p),
-                                                     hist + p * kRadix, lookback + (size_t)p * L.tiles * kRadix,
-                                                     tickets + p);
+        k_onesweep<K, KPT><<<tiles, kSortThreads, smem, s>>>(src_k, src_v, dst_k, dst_v, n, n_dev, 8 * p,
+                                                             pass_mask(key_bits, p), hist + p * kRadix,
+                                                             lookback + (size_t)p * L.tiles * kRadix, tickets + p);
         count_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(src_k, dst_k);
         std::swap(src_v, dst_v);
     }
     if (L.passes & 1) {
-        unsigned cgrid = (unsigned)std::min<size_t>(((size_t)n + kSortBlock - 1) / kSortBlock, 152 * 16);
-        k_copy_back<K><<<cgrid, kSortBlock, 0, s>>>(alt_keys, alt_vals, keys, values, n, n_dev);
+        unsigned cgrid = (unsigned)std::min<size_t>(((size_t)n + 255) / 256, 152 * 16);
+        k_copy_back<K><<<cgrid, 256, 0, s>>>(alt_keys, alt_vals, keys, values, n, n_dev);
         count_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+template <typename K>
+static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
+                             unsigned char* scratch, cudaStream_t s) {
+    SortLayout L = sort_layout(n, key_bits);
+    cudaError_t e;
+    if ((e = sort_prepare()) != cudaSuccess) return e;
+    // Tickets, histograms and look-back states start at zero.
+    if ((e = cudaMemsetAsync(scratch, 0, L.off_keys, s)) != cudaSuccess) return e;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.off_hist);
+    unsigned hgrid = (unsigned)std::min<size_t>(((size_t)n + kHistBlock * 8 - 1) / (kHistBlock * 8),
+                                                (size_t)g_num_sms * 8);
+    if (hgrid == 0) hgrid = 1;
+    launch_hist<K>(keys, n, n_dev, L.passes, key_bits, hist, hgrid, s);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    constexpr bool wide = sizeof(K) == 8;
+    if (use_large_tiles(n, wide))
+        return sort_passes<K, wide ? kKptLarge64 : kKptLarge32>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    return sort_passes<K, wide ? kKptSmall64 : kKptSmall32>(keys, values, n, n_dev, key_bits, L, scratch, s);
 }
 
 cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
