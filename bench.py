@@ -45,19 +45,22 @@ COURTYARD = dict(
 )
 # Shadow rays are generated in the (already reordered) slot order of their
 # path rays and all aim at the light, so the chosen form does not sort them.
+# The chosen form replays each frame as one captured graph with persistent
+# BVH8 traversal; the plain form launches every stage directly (unbatched)
+# with FP32 BVH2 nodes.
 CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=0,
               reorder_shadow_rays=0, use_graph=1)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
-             reorder_shadow_rays=0, use_graph=1)
+             reorder_shadow_rays=0, use_graph=0)
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
-# DRAM bytes (read + write) per ray of the BVH8 traversal launches, from one
-# ncu capture of the 960x540 bounce-1 case (dram__bytes_read.sum +
-# dram__bytes_write.sum over the launch's rays); the traffic of a launch
-# grows with its ray count, so a full launch's traffic is this times its
-# rays.  None until captured.
-TRACE_DRAM_BYTES_PER_RAY = {"any": None, "closest": None}
+# DRAM bytes (read + write) per ray of the full-size bounce-1 BVH8 traversal
+# launches (2,073,600 closest-hit path rays, 4,147,200 any-hit shadow rays),
+# median of 12 launches each from one ncu capture of
+# `bench.py --micro-only` (dram__bytes_read.sum + dram__bytes_write.sum,
+# cold caches): closest 88.9 MB + 10.9 MB, any-hit 154.3 MB + 41.0 MB.
+TRACE_DRAM_BYTES_PER_RAY = {"any": 47.08, "closest": 48.13}
 
 
 def peaks():
@@ -500,6 +503,103 @@ def run_reference(args):
     return out
 
 
+def run_sort_micro(args):
+    """Sort / reorder microbenchmark: stable key-value sorts of 2^16..2^26
+    pairs, u32 and u64 keys, uniform random keys and Morton keys of
+    clustered 6-D Gaussian rays (origins and directions), plus the reorder
+    gather of 32-byte ray records; algorithmic GB/s against the measured HBM
+    peak (passes x 2 x (key + value bytes) per pair for the sort, 80 B per
+    ray for the reorder)."""
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    api = wf.api
+    dev = torch.device("cuda", 0)
+    hbm, peak_kind = peaks()
+    stream = torch.cuda.current_stream()
+    sizes = [int(s) for s in args.sort_sizes.split(",")]
+    gen = torch.Generator(device=dev)
+
+    def timeit(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    def clustered_rays(n):
+        # 64 Gaussian clusters in 6-D: origins in the unit cube, directions
+        # around a cluster axis.
+        gen.manual_seed(n)
+        c = torch.randint(0, 64, (n,), generator=gen, device=dev)
+        co = torch.rand((64, 3), generator=gen, device=dev)
+        cd = torch.nn.functional.normalize(torch.randn((64, 3), generator=gen, device=dev), dim=1)
+        o = (co[c] + 0.05 * torch.randn((n, 3), generator=gen, device=dev)).clamp(0, 1)
+        d = torch.nn.functional.normalize(cd[c] + 0.2 * torch.randn((n, 3), generator=gen, device=dev), dim=1)
+        r = torch.zeros((n, 8), dtype=torch.float32, device=dev)
+        r[:, :3] = o
+        r[:, 4:7] = d
+        r[:, 7] = 1e30
+        return r
+
+    rows = []
+    for n in sizes:
+        rays = clustered_rays(n)
+        reps = 20 if n <= (1 << 22) else 5
+        for bits in (32, 63):
+            wide = bits > 32
+            kdt = torch.int64 if wide else torch.int32
+            keys = torch.empty(n, dtype=kdt, device=dev)
+            ids = torch.empty(n, dtype=torch.int32, device=dev)
+            scratch = torch.empty(api.sort_scratch_bytes(n, 64 if wide else 32), dtype=torch.uint8, device=dev)
+            for dist in ("uniform", "clustered"):
+                if dist == "uniform":
+                    gen.manual_seed(n + bits)
+                    src = torch.randint(0, (1 << 62) if wide else (1 << 32), (n,), generator=gen, device=dev,
+                                        dtype=torch.int64)
+                    src = (src * 2 + (src & 1)) if wide else src.to(torch.int32)
+                else:
+                    kind = wf.MORTON_6D64 if wide else wf.MORTON_AILA32
+                    api.morton(rays, [0, 0, 0], [1, 1, 1], kind, keys, ids)
+                    src = keys.clone()
+                vals = torch.arange(n, dtype=torch.int32, device=dev)
+
+                def one():
+                    keys.copy_(src)
+                    api.sort_pairs(keys, vals, bits, scratch=scratch)
+
+                copy_ms = timeit(lambda: keys.copy_(src), reps)
+                ms = max(timeit(one, reps) - copy_ms, 1e-6)
+                passes = (bits + 7) // 8
+                alg = passes * 2 * ((8 if wide else 4) + 4) * n
+                rows.append({"n": n, "key_bits": bits, "keys": dist, "ms": round(ms, 4),
+                             "gbs": round(alg / (ms * 1e-3) / 1e9, 1), "frac": round(alg / (ms * 1e-3) / 1e9 / hbm, 3)})
+        # Reorder gather of 32-byte ray records by a sorted permutation.
+        # ... by the permutation that sorts the clustered rays' 64-bit keys,
+        # as in the pipeline (Morton -> sort -> reorder).
+        api.morton(rays, [0, 0, 0], [1, 1, 1], wf.MORTON_6D64, keys, ids)
+        api.sort_pairs(keys, ids, 63, scratch=scratch)
+        perm = ids
+        out = torch.empty_like(rays)
+        s2i = torch.arange(n, dtype=torch.int32, device=dev)
+        os2i = torch.empty(n, dtype=torch.int32, device=dev)
+        oi2s = torch.empty(n, dtype=torch.int32, device=dev)
+        ms = timeit(lambda: api.reorder(perm, rays, out, s2i, os2i, oi2s), reps)
+        rows.append({"n": n, "reorder_ms": round(ms, 4), "reorder_gbs": round(80.0 * n / (ms * 1e-3) / 1e9, 1),
+                     "reorder_frac": round(80.0 * n / (ms * 1e-3) / 1e9 / hbm, 3)})
+        del rays, keys, ids, scratch, out
+        torch.cuda.empty_cache()
+    print(json.dumps({"sort_micro": rows, "peak_gbs": hbm, "peak_source": f"{peak_kind} hbm_gbs",
+                      "sort_tiles": api.tune_get("sort.tiles")}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,9 +612,14 @@ def main():
     ap.add_argument("--width", type=int, default=COURTYARD["width"])
     ap.add_argument("--height", type=int, default=COURTYARD["height"])
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")
+    ap.add_argument("--sort-micro", action="store_true", help="sort/reorder microbenchmark over --sort-sizes")
+    ap.add_argument("--sort-sizes", default="65536,262144,1048576,2073600,4194304,16777216,67108864")
     args = ap.parse_args()
     if args.sweep:
         run_sweep(args)
+        return
+    if args.sort_micro:
+        run_sort_micro(args)
         return
     if args.micro_only:
         run_micro_only(args)
