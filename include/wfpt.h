@@ -442,6 +442,45 @@ wfpt_status wfpt_renderer_render(wfpt_renderer* renderer, const wfpt_camera* cam
 /* Ray counts are read back from the device, so this synchronises. */
 wfpt_status wfpt_renderer_get_stats(wfpt_renderer* renderer, wfpt_render_stats* stats);
 
+/* ---- batched render requests (no counterpart in the reference, which
+ * renders one view per Renderer::render call) ---------------------------
+ * Many requests -- different scenes, resolutions, sample counts and depths
+ * -- rendered as one captured CUDA graph: every request's frame is recorded
+ * once, spread over `streams` graph branches so that small requests run
+ * side by side, and each wfpt_batch_render call replays it with every
+ * request's camera and frame index read from device memory.  A request's
+ * output equals what a wfpt_renderer with the same config, scene and camera
+ * renders, frame for frame. */
+typedef struct wfpt_request {
+    const wfpt_scene* scene;
+    const wfpt_geometry* geometries; /* device geometry table of the scene */
+    float light[3];
+    float background[3];
+    wfpt_camera camera;
+    int width, height;
+    wfpt_renderer_config config;     /* use_graph is ignored */
+    float* pixels;                   /* device, width*height float4: accumulated image */
+    float* frame_pixels;             /* device, width*height float4: this frame */
+} wfpt_request;
+
+typedef struct wfpt_batch wfpt_batch;
+
+/* Allocates every request's buffers and records the batch graph (not
+ * inside a stream capture).  streams: graph branches, 1..16. */
+wfpt_status wfpt_batch_create(const wfpt_request* requests, uint32_t count, int streams,
+                              wfpt_batch** batch);
+void wfpt_batch_destroy(wfpt_batch* batch);
+/* One frame of every request, stream-ordered on `stream`.  cameras
+ * (nullable, `count` entries) replaces the requests' cameras for this and
+ * later calls. */
+wfpt_status wfpt_batch_render(wfpt_batch* batch, const wfpt_camera* cameras, void* stream);
+/* Request i's ray counts of the last batch frame (synchronises);
+ * frame_ms is the device time of the whole batch. */
+wfpt_status wfpt_batch_get_stats(wfpt_batch* batch, uint32_t i, wfpt_render_stats* stats);
+/* Kernel launches one wfpt_batch_render makes (the graph's kernel nodes). */
+uint64_t wfpt_batch_kernels(const wfpt_batch* batch);
+void wfpt_batch_reset_frame_index(wfpt_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

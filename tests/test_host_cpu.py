@@ -289,3 +289,18 @@ def test_tuning_knobs(wf):
         api.tune_set("trace.bvh8.refill", old[0])
         api.tune_set("trace.bvh8.postpone", old[1])
         api.tune_set("trace.bvh8.coop", old[2])
+
+
+def test_batch_arguments_rejected_on_host(wf):
+    lib = wf._lib.load()
+    out = C.c_void_p()
+    req = (wf._lib.Request * 1)()
+    assert lib.wfpt_batch_create(req, 0, 1, C.byref(out)) == 1
+    assert lib.wfpt_batch_create(req, 1, 0, C.byref(out)) == 1
+    assert lib.wfpt_batch_create(req, 1, 17, C.byref(out)) == 1
+    assert lib.wfpt_batch_create(req, 1, 2, C.byref(out)) == 1  # null scene
+    assert b"null scene" in lib.wfpt_last_error_message()
+    assert not out
+    st = wf._lib.RenderStats()
+    assert lib.wfpt_batch_get_stats(None, 0, C.byref(st)) == 1
+    assert lib.wfpt_batch_render(None, None, None) == 1

@@ -92,6 +92,21 @@ class RenderStats(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    _fields_ = [
+        ("scene", c_void_p),
+        ("geometries", c_void_p),
+        ("light", c_float * 3),
+        ("background", c_float * 3),
+        ("camera", Camera),
+        ("width", c_int),
+        ("height", c_int),
+        ("config", RendererConfig),
+        ("pixels", c_void_p),
+        ("frame_pixels", c_void_p),
+    ]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [
         ("num_triangles", c_u32),
@@ -151,6 +166,12 @@ _SIGS = {
     "wfpt_renderer_reset_frame_index": (None, [c_void_p]),
     "wfpt_renderer_render": (c_int, [c_void_p, C.POINTER(Camera), c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "wfpt_renderer_get_stats": (c_int, [c_void_p, C.POINTER(RenderStats)]),
+    "wfpt_batch_create": (c_int, [C.POINTER(Request), c_u32, c_int, C.POINTER(c_void_p)]),
+    "wfpt_batch_destroy": (None, [c_void_p]),
+    "wfpt_batch_render": (c_int, [c_void_p, C.POINTER(Camera), c_void_p]),
+    "wfpt_batch_get_stats": (c_int, [c_void_p, c_u32, C.POINTER(RenderStats)]),
+    "wfpt_batch_kernels": (c_u64, [c_void_p]),
+    "wfpt_batch_reset_frame_index": (None, [c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)

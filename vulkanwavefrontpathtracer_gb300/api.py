@@ -343,3 +343,60 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Batched render requests behind the C ABI (wfpt_batch_*): every
+    request's frame recorded once into one CUDA graph over `streams`
+    branches and replayed per render() call.  Each request is a dict with
+    scene (Scene), geometry (Geometry), light, background, camera (Camera),
+    width, height, config (RendererConfig), pixels and frame_pixels (device
+    float tensors of width*height*4)."""
+
+    def __init__(self, requests, streams: int = 4):
+        arr = (L.Request * len(requests))()
+        self._keep = []
+        for i, q in enumerate(requests):
+            r = arr[i]
+            r.scene = q["scene"].handle
+            r.geometries = q["geometry"].table.data_ptr()
+            r.light[:] = [float(x) for x in q["light"]]
+            r.background[:] = [float(x) for x in q["background"]]
+            r.camera = q["camera"]
+            r.width, r.height = int(q["width"]), int(q["height"])
+            r.config = q["config"]
+            r.pixels = q["pixels"].data_ptr()
+            r.frame_pixels = q["frame_pixels"].data_ptr()
+            self._keep.append((q["scene"], q["geometry"], q["pixels"], q["frame_pixels"]))
+        self.count = len(requests)
+        h = C.c_void_p()
+        L.check(lib().wfpt_batch_create(arr, self.count, streams, C.byref(h)))
+        self.handle = h
+
+    def render(self, cameras=None, stream=None):
+        cams = None
+        if cameras is not None:
+            cams = (L.Camera * self.count)(*cameras)
+        L.check(lib().wfpt_batch_render(self.handle, cams, _s(stream)))
+
+    def stats(self, i: int) -> L.RenderStats:
+        st = L.RenderStats()
+        L.check(lib().wfpt_batch_get_stats(self.handle, i, C.byref(st)))
+        return st
+
+    def kernels(self) -> int:
+        return int(lib().wfpt_batch_kernels(self.handle))
+
+    def reset_frame_index(self):
+        lib().wfpt_batch_reset_frame_index(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().wfpt_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -100,6 +100,10 @@ struct wfpt_renderer {
     int width = 0, height = 0;
     int alloc_samples = 0;
     DevBuf i2p, p2i, seeds, decreases, aux, sort_scratch, path_scratch, counters;
+    // Work counters of this renderer's persistent traversal launches (all on
+    // one stream, one after another), so that renderers running
+    // concurrently never share one.
+    DevBuf work;
     RayBufferDev primary, shadow, queue[2];
     uint32_t* host_counters = nullptr;  // pinned
     int last_spp = 0;
@@ -189,7 +193,8 @@ struct wfpt_renderer {
         if (graph) cudaGraphDestroy(graph);
         if (fp_dev) cudaFree(fp_dev);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters}) b->release();
+        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters, &work})
+            b->release();
         primary.release();
         shadow.release();
         queue[0].release();
@@ -198,6 +203,29 @@ struct wfpt_renderer {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (ev2) cudaEventDestroy(ev2);
+    }
+
+    // Ray counts of the last frame from the counters read back to the host
+    // (the caller has waited for that copy).
+    void fill_stats(wfpt_render_stats* st) const {
+        uint64_t n = (uint64_t)width * height;
+        int S = cfg.num_shadow_samples;
+        int rt = cfg.ray_type;
+        for (int p = 0; p < last_spp; ++p) {
+            const uint32_t* c = host_counters + p * kCountersPerPass;
+            st->num_primary_rays += n;
+            if (rt == WFPT_PRIMARY_RAYS) continue;
+            int passes = rt == WFPT_PATH_RAYS ? cfg.recursion_depth + 1 : 1;
+            for (int i = 0; i < passes; ++i) {
+                st->num_shadow_rays += (uint64_t)S * c[kCntHits + i];
+                st->shadow_hits_per_pass[i] += c[kCntHits + i];
+            }
+            if (rt == WFPT_PATH_RAYS)
+                for (int b = 0; b < cfg.recursion_depth; ++b) {
+                    st->num_path_rays += c[kCntPath + b];
+                    st->path_rays_per_bounce[b] += c[kCntPath + b];
+                }
+        }
     }
 
     int key_bits() const {
@@ -237,6 +265,10 @@ struct wfpt_renderer {
         if ((e = sort_scratch.ensure(wfpt::sort_scratch_bytes((uint32_t)sort_n, 64))) != cudaSuccess) return e;
         if ((e = path_scratch.ensure(wfpt::raygen_path_scratch_bytes((uint32_t)n))) != cudaSuccess) return e;
         if ((e = counters.ensure((size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess) return e;
+        if (!work.p) {
+            if ((e = work.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
+            if ((e = cudaMemset(work.p, 0, work.bytes)) != cudaSuccess) return e;
+        }
         if (!host_counters &&
             (e = cudaMallocHost(&host_counters, (size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess)
             return e;
@@ -252,7 +284,7 @@ struct wfpt_renderer {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
         cudaError_t e;
         if (!sort) return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
-                                             n_dev, closest ? 1 : 0, s);
+                                             n_dev, closest ? 1 : 0, s, work.as<uint32_t>());
         float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
         if ((e = wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
                                      rb.idx.as<uint32_t>(), s)) != cudaSuccess)
@@ -267,7 +299,8 @@ struct wfpt_renderer {
             rb.swap();
         }
         return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
-                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s);
+                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s,
+                                  work.as<uint32_t>());
     }
 
     // Renderer::shadowPass (Renderer.cpp:133-154) over input rays `in`
@@ -315,7 +348,8 @@ struct wfpt_renderer {
                                              height, zfar, s, fp, pass, cfg.num_primary_samples)) != cudaSuccess)
             return e;
         if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), cfg.bvh_kind, primary.rays_cur(),
-                                    primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s)) != cudaSuccess)
+                                    primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s,
+                                    work.as<uint32_t>())) != cudaSuccess)
             return e;
         const float one = 1.0f;
         uint32_t one_bits;
@@ -546,26 +580,214 @@ wfpt_status wfpt_renderer_get_stats(wfpt_renderer* r, wfpt_render_stats* st) {
     cudaError_t e = cudaEventSynchronize(r->ev2);
     if (e != cudaSuccess) return wfpt::from_cuda(e);
     cudaEventElapsedTime(&r->frame_ms, r->ev0, r->ev1);
-    uint64_t n = (uint64_t)r->width * r->height;
-    int S = r->cfg.num_shadow_samples;
-    int rt = r->cfg.ray_type;
-    for (int p = 0; p < r->last_spp; ++p) {
-        const uint32_t* c = r->host_counters + p * kCountersPerPass;
-        st->num_primary_rays += n;
-        if (rt == WFPT_PRIMARY_RAYS) continue;
-        int passes = rt == WFPT_PATH_RAYS ? r->cfg.recursion_depth + 1 : 1;
-        for (int i = 0; i < passes; ++i) {
-            st->num_shadow_rays += (uint64_t)S * c[kCntHits + i];
-            st->shadow_hits_per_pass[i] += c[kCntHits + i];
-        }
-        if (rt == WFPT_PATH_RAYS)
-            for (int b = 0; b < r->cfg.recursion_depth; ++b) {
-                st->num_path_rays += c[kCntPath + b];
-                st->path_rays_per_bounce[b] += c[kCntPath + b];
-            }
-    }
+    r->fill_stats(st);
     st->frame_ms = r->frame_ms;
     return WFPT_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ batches
+// Each request gets its own renderer (buffers sized to its resolution,
+// counters, traversal work counters); the batch graph records every
+// renderer's frame plus the read-back of its counters, request i on branch
+// i % streams.
+struct wfpt_batch {
+    std::vector<wfpt_request> reqs;
+    std::vector<wfpt_renderer*> rs;
+    std::vector<cudaStream_t> branches;  // [0] is the capture stream
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+    wfpt::FrameParams* fp_dev = nullptr;
+    std::vector<wfpt::FrameParams> fp_host;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t graph_kernels = 0;
+    bool pending = false;
+    float ms = 0.0f;
+
+    ~wfpt_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (fp_dev) cudaFree(fp_dev);
+        for (cudaEvent_t ev : joins)
+            if (ev) cudaEventDestroy(ev);
+        for (cudaEvent_t ev : {fork, ev0, ev1})
+            if (ev) cudaEventDestroy(ev);
+        for (cudaStream_t s : branches)
+            if (s) cudaStreamDestroy(s);
+        for (wfpt_renderer* r : rs) delete r;
+    }
+
+    // Per-request frame parameters from the current cameras and frame indices.
+    bool fill_params() {
+        for (size_t i = 0; i < reqs.size(); ++i) {
+            const wfpt_request& q = reqs[i];
+            wfpt::FrameParams& p = fp_host[i];
+            std::memset(&p, 0, sizeof(p));
+            if (!wfpt::camera_screen_to_world(q.camera.position, q.camera.rotation_deg, q.camera.fov_deg,
+                                              (float)q.width / (float)q.height, q.camera.znear, q.camera.zfar,
+                                              p.s2w))
+                return false;
+            for (int k = 0; k < 3; ++k) p.eye[k] = q.camera.position[k];
+            p.zfar = q.camera.zfar;
+            p.frame_index = rs[i]->frame_index;
+        }
+        return true;
+    }
+
+    cudaError_t record() {
+        const int K = (int)branches.size();
+        const cudaStream_t cs = branches[0];
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        uint64_t k0 = wfpt::launch_count();
+        cudaError_t fe = cudaEventRecord(fork, cs);
+        for (int k = 1; k < K && fe == cudaSuccess; ++k) fe = cudaStreamWaitEvent(branches[k], fork, 0);
+        for (size_t i = 0; i < reqs.size() && fe == cudaSuccess; ++i) {
+            wfpt_renderer* r = rs[i];
+            const wfpt_request& q = reqs[i];
+            const cudaStream_t s = branches[i % K];
+            const wfpt::FrameParams& p = fp_host[i];
+            fe = r->frame(p.s2w, p.eye, p.zfar, q.pixels, q.frame_pixels, s, fp_dev + i);
+            if (fe == cudaSuccess)
+                fe = cudaMemcpyAsync(r->host_counters, r->counters.p,
+                                     (size_t)r->cfg.num_primary_samples * kCountersPerPass * 4,
+                                     cudaMemcpyDeviceToHost, s);
+        }
+        for (int k = 1; k < K && fe == cudaSuccess; ++k) {
+            fe = cudaEventRecord(joins[k], branches[k]);
+            if (fe == cudaSuccess) fe = cudaStreamWaitEvent(cs, joins[k], 0);
+        }
+        e = cudaStreamEndCapture(cs, &graph);
+        if (fe != cudaSuccess) return fe;
+        if (e != cudaSuccess) return e;
+        graph_kernels = wfpt::launch_count() - k0;
+        return cudaGraphInstantiate(&exec, graph, 0);
+    }
+};
+
+extern "C" {
+
+wfpt_status wfpt_batch_create(const wfpt_request* requests, uint32_t count, int streams, wfpt_batch** batch) {
+    if (!batch) return WFPT_ERR_INVALID_ARGUMENT;
+    *batch = nullptr;
+    if (!requests || count == 0 || streams < 1 || streams > 16) {
+        wfpt::set_error("need requests, count >= 1 and 1 <= streams <= 16");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        const wfpt_request& q = requests[i];
+        if (!q.scene || !q.geometries || !q.pixels || !q.frame_pixels) {
+            wfpt::set_error("request with a null scene, geometry table or image");
+            return WFPT_ERR_INVALID_ARGUMENT;
+        }
+        if (q.width <= 0 || q.height <= 0 || (long long)q.width * q.height > (1ll << 28)) {
+            wfpt::set_error("request with a bad resolution");
+            return WFPT_ERR_INVALID_ARGUMENT;
+        }
+        if (check_config(&q.config) != WFPT_OK) {
+            wfpt::set_error("request option out of range");
+            return WFPT_ERR_INVALID_ARGUMENT;
+        }
+        if (!wfpt::scene_has(q.scene, q.config.bvh_kind)) {
+            wfpt::set_error("request scene was built without the request's BVH kind");
+            return WFPT_ERR_UNSUPPORTED;
+        }
+    }
+    wfpt_batch* b = new (std::nothrow) wfpt_batch();
+    if (!b) return WFPT_ERR_OUT_OF_MEMORY;
+    b->reqs.assign(requests, requests + count);
+    b->fp_host.resize(count);
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < count && e == cudaSuccess; ++i) {
+        wfpt_renderer* r = new (std::nothrow) wfpt_renderer();
+        if (!r) {
+            delete b;
+            return WFPT_ERR_OUT_OF_MEMORY;
+        }
+        b->rs.push_back(r);
+        const wfpt_request& q = b->reqs[i];
+        r->cfg = q.config;
+        r->cfg.use_graph = 0;
+        r->scene = q.scene;
+        r->geoms = q.geometries;
+        wfpt::scene_bounds(q.scene, r->smin, r->smax);
+        for (int k = 0; k < 3; ++k) {
+            r->light[k] = q.light[k];
+            r->bg[k] = q.background[k];
+        }
+        e = r->prepare(q.width, q.height);
+        r->last_spp = r->cfg.num_primary_samples;
+    }
+    b->branches.assign((size_t)streams, nullptr);
+    b->joins.assign((size_t)streams, nullptr);
+    for (int k = 0; k < streams && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&b->branches[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess && k > 0) e = cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->fp_dev, (size_t)count * sizeof(wfpt::FrameParams));
+    if (e == cudaSuccess) e = wfpt::sort_prepare();
+    if (e == cudaSuccess) e = wfpt::trace_prepare();
+    if (e == cudaSuccess && !b->fill_params()) {
+        delete b;
+        wfpt::set_error("request with a bad camera");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    if (e == cudaSuccess) e = b->record();
+    if (e != cudaSuccess) {
+        delete b;
+        return wfpt::from_cuda(e);
+    }
+    *batch = b;
+    return WFPT_OK;
+}
+
+void wfpt_batch_destroy(wfpt_batch* batch) { delete batch; }
+
+wfpt_status wfpt_batch_render(wfpt_batch* b, const wfpt_camera* cameras, void* stream) {
+    if (!b) return WFPT_ERR_INVALID_ARGUMENT;
+    if (cameras)
+        for (size_t i = 0; i < b->reqs.size(); ++i) b->reqs[i].camera = cameras[i];
+    if (!b->fill_params()) {
+        wfpt::set_error("bad camera");
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if ((e = cudaEventRecord(b->ev0, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    // Pageable source: the copy is staged before the call returns.
+    if ((e = cudaMemcpyAsync(b->fp_dev, b->fp_host.data(), b->fp_host.size() * sizeof(wfpt::FrameParams),
+                             cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return wfpt::from_cuda(e);
+    if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    if ((e = cudaEventRecord(b->ev1, s)) != cudaSuccess) return wfpt::from_cuda(e);
+    wfpt::count_launch((uint32_t)b->graph_kernels);
+    for (wfpt_renderer* r : b->rs) ++r->frame_index;
+    b->pending = true;
+    return WFPT_OK;
+}
+
+wfpt_status wfpt_batch_get_stats(wfpt_batch* b, uint32_t i, wfpt_render_stats* st) {
+    if (!b || !st || i >= b->rs.size()) return WFPT_ERR_INVALID_ARGUMENT;
+    std::memset(st, 0, sizeof(*st));
+    if (!b->pending) return WFPT_OK;
+    cudaError_t e = cudaEventSynchronize(b->ev1);
+    if (e != cudaSuccess) return wfpt::from_cuda(e);
+    cudaEventElapsedTime(&b->ms, b->ev0, b->ev1);
+    b->rs[i]->fill_stats(st);
+    st->frame_ms = b->ms;
+    return WFPT_OK;
+}
+
+uint64_t wfpt_batch_kernels(const wfpt_batch* b) { return b ? b->graph_kernels : 0; }
+
+void wfpt_batch_reset_frame_index(wfpt_batch* b) {
+    if (!b) return;
+    for (wfpt_renderer* r : b->rs) r->frame_index = 1;
 }
 
 }  // extern "C"

@@ -794,7 +794,7 @@ uint32_t get_trace_postpone() { return g_postpone; }
 
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
-                         cudaStream_t s) {
+                         cudaStream_t s, uint32_t* own_work) {
     if (n == 0) return cudaSuccess;
     unsigned grid = (n + kBlock - 1) / kBlock;
     const float4* rr = reinterpret_cast<const float4*>(rays);
@@ -809,7 +809,7 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
         unsigned pgrid = (unsigned)(g_num_sms * g_blocks_per_sm[(coop ? 2 : 0) + (closest ? 1 : 0)]);
         if (pgrid == 0) pgrid = 1;
         if (grid < pgrid) pgrid = grid;
-        uint32_t* work = sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
+        uint32_t* work = own_work ? own_work : sc.work + 16 * (g_slot.fetch_add(1) % kWorkSlots);
         if (coop) {
             auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
                               : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);

@@ -27,8 +27,12 @@ bool get_trace_count();
 cudaError_t trace_counters(uint64_t out[4], bool reset);
 cudaError_t trace_prepare();
 
+// work (nullable): the persistent BVH8 kernel's two self-resetting work
+// counters (zeroed once by the owner); launches that use the same counters
+// must be ordered one after another.  Null takes the next of the scene's
+// counter slots.
 cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, wfpt_hit* results,
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
-                         cudaStream_t s);
+                         cudaStream_t s, uint32_t* work = nullptr);
 
 }  // namespace wfpt
