@@ -503,6 +503,99 @@ def run_reference(args):
     return out
 
 
+# Batched serving workload: 64 requests over 4 seeded scenes (65,536-triangle
+# soup, the 268,304-triangle courtyard, a ~1M-triangle and the 3M-triangle
+# city block), resolutions drawn from {128^2, 256^2, 512^2, 1024^2}, 1-16
+# samples per pixel and depth 1-8, path rays, chosen form.
+BATCH_SCENES = [
+    dict(kind=0, seed=1, ntris=65536, light=(0.5, 1.6, 0.5), background=(0.53, 0.81, 0.98),
+         camera=dict(position=(0.5, 0.5, 2.2), rotation_deg=(0.0, 0.0, 0.0), fov_deg=45.0, znear=0.001,
+                     zfar=10.0)),
+    dict(kind=1, seed=1, ntris=0, light=COURTYARD["light"], background=COURTYARD["background"],
+         camera=COURTYARD["camera"]),
+    dict(kind=3, seed=1, ntris=1000000, light=(185.0, 300.0, 185.0), background=(0.53, 0.81, 0.98),
+         camera=dict(position=(185.0, 60.0, 420.0), rotation_deg=(-12.0, 0.0, 0.0), fov_deg=60.0, znear=0.1,
+                     zfar=2000.0)),
+    dict(kind=2, seed=1, ntris=0, light=(320.0, 400.0, 320.0), background=(0.53, 0.81, 0.98),
+         camera=dict(position=(320.0, 80.0, 720.0), rotation_deg=(-12.0, 0.0, 0.0), fov_deg=60.0, znear=0.1,
+                     zfar=3000.0)),
+]
+
+
+def batch_requests(seed=7, count=64):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        res = int(rng.choice([128, 256, 512, 1024]))
+        out.append(dict(scene=int(rng.integers(0, 4)), width=res, height=res, spp=int(rng.integers(1, 17)),
+                        depth=int(rng.integers(1, 9))))
+    return out
+
+
+def run_batched(args):
+    """One step = one frame of all 64 requests: batched (one graph replay,
+    4 branches) against the same requests rendered one after another
+    through standalone renderers with every stage launched directly."""
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    api = wf.api
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    scenes = []
+    for s in BATCH_SCENES:
+        pos, nrm, idx = api.generate_scene(s["kind"], s["seed"], s["ntris"])
+        scenes.append((api.Scene(pos, idx), api.Geometry(pos, nrm, idx, device=dev), int(idx.shape[0])))
+    specs = batch_requests(count=args.batch_requests)
+    reqs, solos = [], []
+    for q in specs:
+        s = BATCH_SCENES[q["scene"]]
+        sc, geom, _ = scenes[q["scene"]]
+        over = dict(COURTYARD["renderer"], num_primary_samples=q["spp"], recursion_depth=q["depth"],
+                    shadow_radius=COURTYARD["renderer"]["shadow_radius"] if q["scene"] != 0 else 0.1)
+        n = q["width"] * q["height"]
+        px = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        fp = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        reqs.append(dict(scene=sc, geometry=geom, light=s["light"], background=s["background"],
+                         camera=api.make_camera(**s["camera"]), width=q["width"], height=q["height"],
+                         config=api.default_config(**over, **CHOSEN), pixels=px, frame_pixels=fp))
+        solo = api.Renderer(**over, **dict(CHOSEN, use_graph=0))
+        solo.set_scene(sc, geom, s["light"], s["background"])
+        solos.append((solo, api.make_camera(**s["camera"]), q["width"], q["height"], px, fp))
+    batch = api.Batch(reqs, streams=4)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    def solo_all():
+        for r, cam, w, h, px, fp in solos:
+            r.render(cam, w, h, px, fp)
+
+    ms_batch = timed(batch.render, args.steps, args.warmup)
+    rays = sum(st.num_primary_rays + st.num_shadow_rays + st.num_path_rays
+               for st in (batch.stats(i) for i in range(len(reqs))))
+    ms_solo = timed(solo_all, max(1, args.steps // 2), 1)
+    out = {"metric": "Mrays/s, batched render requests (chosen form)", "value": round(rays / (ms_batch * 1e-3) / 1e6, 3),
+           "unit": "Mrays/s", "ms_per_step": round(ms_batch, 3), "steps": args.steps, "warmup": args.warmup,
+           "requests": len(reqs), "rays_per_step": int(rays), "graph_kernels": batch.kernels(),
+           "unbatched": {"value": round(rays / (ms_solo * 1e-3) / 1e6, 3), "ms_per_step": round(ms_solo, 3)},
+           "batched_over_unbatched": round(ms_solo / ms_batch, 3),
+           "scenes_triangles": [s[2] for s in scenes],
+           "requests_by_resolution": {str(r): sum(1 for q in specs if q["width"] == r) for r in (128, 256, 512, 1024)}}
+    print(json.dumps(out))
+
+
 def run_sort_micro(args):
     """Sort / reorder microbenchmark: stable key-value sorts of 2^16..2^26
     pairs, u32 and u64 keys, uniform random keys and Morton keys of
@@ -614,7 +707,12 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")
     ap.add_argument("--sort-micro", action="store_true", help="sort/reorder microbenchmark over --sort-sizes")
     ap.add_argument("--sort-sizes", default="65536,262144,1048576,2073600,4194304,16777216,67108864")
+    ap.add_argument("--batched", action="store_true", help="the 64-request batched serving workload")
+    ap.add_argument("--batch-requests", type=int, default=64)
     args = ap.parse_args()
+    if args.batched:
+        run_batched(args)
+        return
     if args.sweep:
         run_sweep(args)
         return
