@@ -198,7 +198,10 @@ wfpt_status wfpt_sort_pairs(void* keys, uint32_t* values, uint32_t n,
 
 /* reorderRays.comp:27-46 + Tracer::reorderRays (Tracer.cpp:80-98):
  * out_rays[i] = in_rays[idx[i]]; out_slot_to_index[i] =
- * in_slot_to_index[idx[i]]; out_index_to_slot[out_slot_to_index[i]] = i. */
+ * in_slot_to_index[idx[i]]; out_index_to_slot[out_slot_to_index[i]] = i.
+ * ray_index must be a permutation of [0, n); out_index_to_slot must have
+ * room for every value in in_slot_to_index (pixel indices in a renderer,
+ * which can exceed n in a compacted wavefront). */
 wfpt_status wfpt_reorder(const uint32_t* ray_index, const wfpt_ray* in_rays,
                          wfpt_ray* out_rays, const int32_t* in_slot_to_index,
                          int32_t* out_slot_to_index, int32_t* out_index_to_slot,
@@ -359,6 +362,28 @@ wfpt_status wfpt_scene_export_bvh8(const wfpt_scene* scene, void* nodes,
 wfpt_status wfpt_trace(const wfpt_scene* scene, int bvh_kind, const wfpt_ray* rays,
                        wfpt_hit* results, const uint32_t* ray_index, uint32_t n,
                        const uint32_t* n_dev, int closest_hit, void* stream);
+
+/* Tracer::traceSort (Tracer.cpp:214-225) as one stream-ordered call:
+ * Morton keys of the rays over the box [scene_min, scene_max] (wfpt_morton
+ * with morton_kind), stable key sort of (key, index) (wfpt_sort_pairs with
+ * 32, 48 or 63 key bits), then
+ *  - reorder != 0: wfpt_reorder into rays_out / slot_to_index_out /
+ *    index_to_slot_out and trace those (the reordered buffers become the
+ *    wavefront, as RayBuffer::swap does); results follow the reordered
+ *    slots;
+ *  - reorder == 0: trace the rays in sorted order through the indirect
+ *    index; results land at each ray's own slot (rays_out and the out maps
+ *    may be null).
+ * keys: n u32 (WFPT_MORTON_AILA32) or n u64 (6-D kinds); indices: n u32;
+ * scratch: at least wfpt_sort_scratch_bytes(n, 64) bytes. */
+wfpt_status wfpt_trace_sort(const wfpt_scene* scene, int bvh_kind, const wfpt_ray* rays,
+                            wfpt_hit* results, uint32_t n, const uint32_t* n_dev,
+                            const float scene_min[3], const float scene_max[3],
+                            int morton_kind, int reorder, wfpt_ray* rays_out,
+                            const int32_t* slot_to_index, int32_t* slot_to_index_out,
+                            int32_t* index_to_slot_out, void* keys, uint32_t* indices,
+                            int closest_hit, void* scratch, size_t scratch_bytes,
+                            void* stream);
 
 /* ------------------------------------------------------ synthetic scenes */
 

@@ -232,3 +232,40 @@ def test_city_3m_triangles_against_fp64(wf, orc, dev):
     t32 = g8[both, 2].view(np.float32).astype(np.float64)
     assert np.all(np.abs(t32 - t64[both]) <= 1e-5 * t64[both] + 1e-6 * extent)
     assert wf.api.device_status() == 0
+
+
+@pytest.mark.parametrize("morton_kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1])
+def test_trace_sort_composite(wf, dev, courtyard, kind, morton_kind):
+    """wfpt_trace_sort (Tracer::traceSort): indirect results equal a plain
+    trace at every slot; reordered results equal the plain hit of the ray
+    that sorted into each slot, and the slot maps follow the rays."""
+    import torch
+    pos, idx, sc = courtyard
+    rng = np.random.default_rng(40 + morton_kind)
+    n = 123457
+    rays = random_rays(rng, n, tmax=1e30)
+    rays[:, :3] = rng.uniform(sc.bounds_min, sc.bounds_max, (n, 3)).astype(np.float32)
+    plain = gpu_trace(wf, dev, sc, kind, rays)
+    d_rays = T(rays, dev)
+    res = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    keys = torch.empty(n, dtype=torch.int64, device=dev)
+    ids = torch.empty(n, dtype=torch.int32, device=dev)
+    wf.api.trace_sort(sc, kind, d_rays, res, sc.bounds_min, sc.bounds_max, morton_kind, False, keys, ids)
+    assert np.array_equal(N(res), plain)
+    out = torch.empty_like(d_rays)
+    # Slot -> index map: a permutation of [0, n) (pixel indices in the
+    # renderer); the reorder writes index_to_slot_out at these values.
+    perm = rng.permutation(n).astype(np.int32)
+    s2i = T(perm, dev)
+    os2i = torch.empty(n, dtype=torch.int32, device=dev)
+    oi2s = torch.empty(n, dtype=torch.int32, device=dev)
+    wf.api.trace_sort(sc, kind, d_rays, res, sc.bounds_min, sc.bounds_max, morton_kind, True, keys, ids,
+                      rays_out=out, slot_to_index=s2i, slot_to_index_out=os2i, index_to_slot_out=oi2s)
+    order = N(ids).view(np.uint32)
+    assert np.array_equal(np.sort(order), np.arange(n))
+    assert np.array_equal(N(res), plain[order])
+    assert np.array_equal(N(out), rays[order])
+    assert np.array_equal(N(os2i), perm[order])
+    assert np.array_equal(N(oi2s)[perm[order]], np.arange(n))
+    assert wf.api.device_status() == 0

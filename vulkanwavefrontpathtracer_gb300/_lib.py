@@ -157,7 +157,10 @@ _SIGS = {
     "wfpt_scene_export_bvh2": (c_int, [c_void_p, c_void_p, P_size, c_void_p, P_size]),
     "wfpt_scene_export_bvh8": (c_int, [c_void_p, c_void_p, P_size, c_void_p, P_size]),
     "wfpt_trace": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_u32, c_void_p, c_int, c_void_p]),
-    "wfpt_generate_scene": (c_int, [c_int, c_u64, c_u32, c_void_p, c_void_p, P_u32, c_void_p, P_u32]),
+    "wfpt_trace_sort": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_u32, c_void_p, P_f32, P_f32, c_int, c_int,
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                c_size_t, c_void_p]),
+    "wfpt_generate_scene":(c_int, [c_int, c_u64, c_u32, c_void_p, c_void_p, P_u32, c_void_p, P_u32]),
     "wfpt_renderer_config_default": (None, [C.POINTER(RendererConfig)]),
     "wfpt_renderer_create": (c_int, [C.POINTER(RendererConfig), C.POINTER(c_void_p)]),
     "wfpt_renderer_destroy": (None, [c_void_p]),

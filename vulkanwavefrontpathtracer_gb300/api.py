@@ -127,6 +127,21 @@ def trace(scene: "Scene", bvh_kind, rays, results, ray_index=None, closest_hit=T
                              1 if closest_hit else 0, _s(stream)))
 
 
+def trace_sort(scene: "Scene", bvh_kind, rays, results, scene_min, scene_max, morton_kind, reorder, keys, indices,
+               rays_out=None, slot_to_index=None, slot_to_index_out=None, index_to_slot_out=None, closest_hit=True,
+               scratch=None, n=None, n_dev=None, stream=None):
+    """Tracer::traceSort: Morton -> sort -> reorder (or indirect) -> trace."""
+    n = _n(rays, n)
+    if scratch is None:
+        scratch = torch.empty(max(sort_scratch_bytes(n, 64), 1), dtype=torch.uint8, device=rays.device)
+    L.check(lib().wfpt_trace_sort(scene.handle, bvh_kind, _p(rays), _p(results), n, _p(n_dev),
+                                  L.fvec(scene_min, 3), L.fvec(scene_max, 3), morton_kind, 1 if reorder else 0,
+                                  _p(rays_out), _p(slot_to_index), _p(slot_to_index_out), _p(index_to_slot_out),
+                                  _p(keys), _p(indices), 1 if closest_hit else 0, _p(scratch), scratch.numel(),
+                                  _s(stream)))
+    return scratch
+
+
 def raygen_shadow(seeds, in_rays, in_results, out_rays, out_slot_to_index, out_index_to_slot, light, light_radius,
                   batch_begin, batch_size, num_samples, n_in_dev=None, stream=None):
     L.check(lib().wfpt_raygen_shadow(_p(seeds), _p(in_rays), _p(in_results), _p(out_rays), _p(out_slot_to_index),

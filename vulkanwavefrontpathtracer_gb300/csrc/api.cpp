@@ -524,6 +524,30 @@ wfpt_status wfpt_trace(const wfpt_scene* scene, int bvh_kind, const wfpt_ray* ra
                                         S(stream)));
 }
 
+wfpt_status wfpt_trace_sort(const wfpt_scene* scene, int bvh_kind, const wfpt_ray* rays, wfpt_hit* results,
+                            uint32_t n, const uint32_t* n_dev, const float scene_min[3], const float scene_max[3],
+                            int morton_kind, int reorder, wfpt_ray* rays_out, const int32_t* slot_to_index,
+                            int32_t* slot_to_index_out, int32_t* index_to_slot_out, void* keys, uint32_t* indices,
+                            int closest_hit, void* scratch, size_t scratch_bytes, void* stream) {
+    WFPT_REQUIRE(scene_min && scene_max, "null scene box");
+    WFPT_REQUIRE(morton_kind >= WFPT_MORTON_AILA32 && morton_kind <= WFPT_MORTON_6D64, "unknown morton kind");
+    WFPT_REQUIRE(!reorder || n == 0 || (rays_out && slot_to_index && slot_to_index_out && index_to_slot_out),
+                 "reorder needs the output rays and slot maps");
+    const int key_bits = morton_kind == WFPT_MORTON_AILA32 ? 32 : (morton_kind == WFPT_MORTON_6D48 ? 48 : 63);
+    const float size[3] = {scene_max[0] - scene_min[0], scene_max[1] - scene_min[1], scene_max[2] - scene_min[2]};
+    wfpt_status st = wfpt_morton(rays, n, n_dev, scene_min, size, morton_kind, keys, indices, stream);
+    if (st != WFPT_OK) return st;
+    if ((st = wfpt_sort_pairs(keys, indices, n, n_dev, key_bits, scratch, scratch_bytes, stream)) != WFPT_OK)
+        return st;
+    if (reorder) {
+        if ((st = wfpt_reorder(indices, rays, rays_out, slot_to_index, slot_to_index_out, index_to_slot_out, n, n_dev,
+                               stream)) != WFPT_OK)
+            return st;
+        return wfpt_trace(scene, bvh_kind, rays_out, results, nullptr, n, n_dev, closest_hit, stream);
+    }
+    return wfpt_trace(scene, bvh_kind, rays, results, indices, n, n_dev, closest_hit, stream);
+}
+
 wfpt_status wfpt_generate_scene(int kind, uint64_t seed, uint32_t num_triangles, float* positions, float* normals,
                                 uint32_t* num_vertices, uint32_t* indices, uint32_t* num_triangles_out) {
     WFPT_REQUIRE(num_vertices && num_triangles_out, "null count pointer");
