@@ -232,12 +232,17 @@ def gltf_vertices(positions: np.ndarray, normals: np.ndarray) -> np.ndarray:
 
 class Geometry:
     """Device-side shading geometry: vertex buffer, index buffer and the
-    one-entry geometry table {vertexAddr, indexAddr} (geometrytypes.glsl:9-12)."""
+    geometry table {vertexAddr, indexAddr} (geometrytypes.glsl:9-12), one
+    entry per geometry; geometry_first[g] (nullable: one geometry) is its
+    first triangle, and its index address is pre-offset to it, as the
+    reference offsets by firstIndex (WaveFrontPathTracer.cpp:268-271)."""
 
-    def __init__(self, positions, normals, indices, device="cuda"):
+    def __init__(self, positions, normals, indices, device="cuda", geometry_first=None):
         self.vertices = torch.from_numpy(gltf_vertices(positions, normals)).to(device)
         self.indices = torch.from_numpy(np.ascontiguousarray(indices).view(np.int32).reshape(-1)).to(device)
-        table = np.array([[self.vertices.data_ptr(), self.indices.data_ptr()]], dtype=np.uint64)
+        first = [0] if geometry_first is None else [int(x) for x in geometry_first]
+        table = np.array([[self.vertices.data_ptr(), self.indices.data_ptr() + 12 * f] for f in first],
+                         dtype=np.uint64)
         self.table = torch.from_numpy(table.view(np.int64)).to(device)
         self.host_vertices = gltf_vertices(positions, normals)
         self.host_indices = np.ascontiguousarray(indices, np.uint32)
