@@ -214,6 +214,8 @@ def run_ours(args):
     out = None
     if rank == 0:
         cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
+        if cpu is not None:
+            cpu["stages"] = cpu_stages(wf, api, dev, scene, geom, cam)
         def trace_roof(tr, kernel, kind):
             ach = tr["alg_bytes"] / (tr["ms"] * 1e-3) / 1e9
             per_ray = TRACE_DRAM_BYTES_PER_RAY[kind]
@@ -456,6 +458,42 @@ def cpu_frame(args, api, scene, pos, nrm, idx, w, h, form):
                                    W["background"], s2w, c["position"], c["zfar"], w, h, cfg)
     dt = time.perf_counter() - t0
     return (st.primary + st.shadow + st.path), dt
+
+
+def cpu_stages(wf, api, dev, scene, geom, cam, n_sample=1 << 20):
+    """Per-stage CPU oracle throughput on a 1M-ray sample of the bounce-1
+    path wavefront and its shadow rays (the same rays the GPU per-bounce
+    line traces): Morton keys, stable sort, reorder, closest-hit and any-hit
+    traversal of the FP32 BVH2."""
+    import oracle
+    W = COURTYARD
+    path, shadow = make_wavefronts(wf, api, dev, scene, geom, cam, W["width"], W["height"], W["light"])
+    p = path[:n_sample].cpu().numpy()
+    s = shadow[:n_sample].cpu().numpy()
+    nodes, tris = scene.export_bvh2()
+    smin, ssize = scene.bounds_min, scene.bounds_max - scene.bounds_min
+    th = oracle.num_threads()
+    out = {}
+
+    def timed(fn):
+        t = time.perf_counter()
+        r = fn()
+        return r, time.perf_counter() - t
+
+    (keys, ids), dt = timed(lambda: oracle.morton(p, smin, ssize, 2))
+    out["morton_6d64"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "threads": th}
+    (_, order), dt = timed(lambda: oracle.sort_pairs(keys, ids, 63))
+    out["sort_u64_63bit"] = {"mpairs_s": round(p.shape[0] / dt / 1e6, 2), "gbs": round(192.0 * p.shape[0] / dt / 1e9, 3),
+                             "threads": 1}
+    _, dt = timed(lambda: oracle.reorder(order, p, np.arange(p.shape[0], dtype=np.int32)))
+    out["reorder"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "gbs": round(80.0 * p.shape[0] / dt / 1e9, 3),
+                      "threads": 1}
+    _, dt = timed(lambda: oracle.trace_bvh2(nodes, tris, p, closest=True))
+    out["trace_closest"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "threads": th}
+    _, dt = timed(lambda: oracle.trace_bvh2(nodes, tris, s, closest=False))
+    out["trace_any"] = {"mrays_s": round(s.shape[0] / dt / 1e6, 2), "threads": th}
+    out["sample"] = f"{p.shape[0]} bounce-1 path rays and {s.shape[0]} shadow rays of the courtyard frame"
+    return out
 
 
 def cpu_baseline(args, wf, api, scene, pos, nrm, idx):

@@ -281,11 +281,12 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh2(const float4* __restrict_
 // --------------------------------------------------------- BVH8 (chosen)
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xFFu; }
 
-// Byte b of w as an exact float: the byte is permuted into the mantissa of
-// 2^23 (bits 0x4B000000), then 2^23 is subtracted -- one PRMT and one FADD
-// instead of an integer-to-float conversion.
+// Byte b of w as the exact float 2^15 + q: one PRMT places the byte in
+// mantissa bits 8..15 of 2^15 (bits 0x4700qq00).  The 2^15 bias is folded
+// into the node's slab offsets (intersect_node8), so a plane costs one PRMT
+// and one FMA.
 __device__ __forceinline__ float q2f(uint32_t w, int b) {
-    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)b)), 8388608.0f);
+    return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7604u | ((uint32_t)b << 4)));
 }
 
 // Intersects the eight children of a BVH8 node.  Returns the hit mask:
@@ -306,11 +307,24 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
     imask = ew >> 24;
     child_base = __float_as_uint(n1.x);
     tri_base = __float_as_uint(n1.y);
-    // Slab distance = q * (scale*inv) + (p - o) * inv.
+    // Slab distance = q * (scale*inv) + (p - o) * inv, evaluated as
+    // (2^15 + q) * a + (b - 2^15 a).  The folded offset is rounded twice
+    // (about 2^-24 * (|b| + 2^15 |a|) each); near planes move earlier and far
+    // planes later by m = 2^-7 |a| + 2^-22 |b|, which covers that with room
+    // to spare (2^-7 of a quantisation step), so culling stays as
+    // conservative as the unfolded form.
     float ax = __fmul_rn(scx, r.inv.x), ay = __fmul_rn(scy, r.inv.y), az = __fmul_rn(scz, r.inv.z);
-    float bx = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
-    float by = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
-    float bz = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
+    const float bx0 = __fmaf_rn(n0.x, r.inv.x, -r.oinv.x);
+    const float by0 = __fmaf_rn(n0.y, r.inv.y, -r.oinv.y);
+    const float bz0 = __fmaf_rn(n0.z, r.inv.z, -r.oinv.z);
+    const float mx = __fmaf_rn(fabsf(bx0), 0x1p-22f, __fmul_rn(fabsf(ax), 0x1p-7f));
+    const float my = __fmaf_rn(fabsf(by0), 0x1p-22f, __fmul_rn(fabsf(ay), 0x1p-7f));
+    const float mz = __fmaf_rn(fabsf(bz0), 0x1p-22f, __fmul_rn(fabsf(az), 0x1p-7f));
+    const float fx0 = __fmaf_rn(-32768.0f, ax, bx0), fy0 = __fmaf_rn(-32768.0f, ay, by0);
+    const float fz0 = __fmaf_rn(-32768.0f, az, bz0);
+    const float bxn = __fsub_rn(fx0, mx), bxf = __fadd_rn(fx0, mx);
+    const float byn = __fsub_rn(fy0, my), byf = __fadd_rn(fy0, my);
+    const float bzn = __fsub_rn(fz0, mz), bzf = __fadd_rn(fz0, mz);
     // Near/far planes per axis chosen once per node by the ray octant
     // (d < 0: the hi plane is entered first).
     const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
@@ -337,9 +351,9 @@ __device__ __forceinline__ uint32_t intersect_node8(const float4* __restrict__ n
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int w = c >> 2, b = c & 3;
-        float tnx = __fmaf_rn(q2f(nx[w], b), ax, bx), tfx = __fmaf_rn(q2f(fx[w], b), ax, bx);
-        float tny = __fmaf_rn(q2f(ny[w], b), ay, by), tfy = __fmaf_rn(q2f(fy[w], b), ay, by);
-        float tnz = __fmaf_rn(q2f(nz[w], b), az, bz), tfz = __fmaf_rn(q2f(fz[w], b), az, bz);
+        float tnx = __fmaf_rn(q2f(nx[w], b), ax, bxn), tfx = __fmaf_rn(q2f(fx[w], b), ax, bxf);
+        float tny = __fmaf_rn(q2f(ny[w], b), ay, byn), tfy = __fmaf_rn(q2f(fy[w], b), ay, byf);
+        float tnz = __fmaf_rn(q2f(nz[w], b), az, bzn), tfz = __fmaf_rn(q2f(fz[w], b), az, bzf);
         float tn = fmaxf(max3f(tnx, tny, tnz), r.tmin);
         float tf = fminf(min3f(tfx, tfy, tfz), tcur);
         if (tn <= tf * kBoxSlack) hit8 |= 1u << c;
