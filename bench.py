@@ -52,6 +52,9 @@ CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, 
               reorder_shadow_rays=0, use_graph=1)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
              reorder_shadow_rays=0, use_graph=0)
+# Per-bounce reordering mask chosen by autotune.tune_bounce_sort on this
+# workload (bench.py --sweep): every bounce traces unsorted.
+TUNED_PATH_SORT_SKIP = 0xFF
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
@@ -190,6 +193,11 @@ def run_ours(args):
     ms_p, rays_p, st_p, _ = timed_frames(plain, args.steps, max(1, args.warmup // 2))
     value = rays_c / (ms_c * 1e-3) / 1e6
     plain_value = rays_p / (ms_p * 1e-3) / 1e6
+    # The autotuner's per-bounce reordering choice for this scene (bench.py
+    # --sweep, bounce_sort): no bounce's sort pays for itself.
+    tuned = make(dict(CHOSEN, path_sort_skip=TUNED_PATH_SORT_SKIP))
+    ms_t, rays_t, _, _ = timed_frames(tuned, args.steps, max(1, args.warmup // 2))
+    tuned_value = rays_t / (ms_t * 1e-3) / 1e6
 
     # End to end through the C ABI with host buffers: per step the frame is
     # rendered and the tone-mapped image is read back into pinned memory.
@@ -244,6 +252,9 @@ def run_ours(args):
             "plain": {"value": round(plain_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_p / args.steps, 4),
                       "rays_per_frame": int(st_p.num_primary_rays + st_p.num_shadow_rays + st_p.num_path_rays)},
             "chosen_over_plain": round(value / plain_value, 3),
+            "autotuned": {"value": round(tuned_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_t / args.steps, 4),
+                          "path_sort_skip": TUNED_PATH_SORT_SKIP, "over_plain": round(tuned_value / plain_value, 3),
+                          "note": "chosen form with the autotuned per-bounce reordering"},
             "per_bounce": micro["per_bounce"],
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),
@@ -418,7 +429,15 @@ def run_sweep(args):
     work = {f"{form}_{kind}": autotune.measure_work(scene, rays, bvh, closest)
             for form, bvh in (("bvh2", wf.BVH2_FP32), ("bvh8", wf.BVH8_Q8))
             for kind, rays, closest in (("path", path, True), ("shadow", shadow, False))}
-    print(json.dumps({"keys": keys, "traversal": trav, "work": work, "resolution": [args.width, args.height]}))
+
+    def make_renderer(mask):
+        r = api.Renderer(**W["renderer"], **dict(CHOSEN, path_sort_skip=mask))
+        r.set_scene(scene, geom, W["light"], W["background"])
+        return r
+
+    bounces = autotune.tune_bounce_sort(make_renderer, cam, args.width, args.height, W["renderer"]["recursion_depth"])
+    print(json.dumps({"keys": keys, "traversal": trav, "work": work, "bounce_sort": bounces,
+                      "resolution": [args.width, args.height]}))
 
 
 def run_micro_only(args):

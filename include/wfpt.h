@@ -423,6 +423,9 @@ typedef struct wfpt_renderer_config {
     int bvh_kind;                   /* wfpt_bvh_kind used by trace */
     float albedo;                   /* path albedo, reference hard-codes 0.8 */
     int use_graph;                  /* capture the frame in a CUDA graph */
+    int path_sort_skip;             /* bit b set: bounce b+1 traces its path rays
+                                       unsorted even when sort_path_rays is on
+                                       (per-bounce reordering; 0..255, default 0) */
 } wfpt_renderer_config;
 
 void wfpt_renderer_config_default(wfpt_renderer_config* config);

@@ -22,7 +22,8 @@ class FrameCfg(C.Structure):
     _fields_ = [("ray_type", C.c_int), ("spp", C.c_int), ("S", C.c_int), ("depth", C.c_int),
                 ("radius", C.c_float), ("key", C.c_float), ("white", C.c_float), ("albedo", C.c_float),
                 ("sort_shadow", C.c_int), ("reorder_shadow", C.c_int), ("sort_path", C.c_int),
-                ("reorder_path", C.c_int), ("morton_kind", C.c_int), ("frame_index", C.c_int)]
+                ("reorder_path", C.c_int), ("morton_kind", C.c_int), ("frame_index", C.c_int),
+                ("path_sort_skip", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -943,6 +943,7 @@ struct OFrameCfg {
     float radius, key, white, albedo;
     int sort_shadow, reorder_shadow, sort_path, reorder_path, morton_kind;
     int frame_index;
+    int path_sort_skip;  // bit b: bounce b+1 traces its path rays unsorted
 };
 
 struct OStats {
@@ -1051,8 +1052,9 @@ extern "C" void orc_render_frame(const void* nodes, const void* tris, const OGeo
             stats->path += cnt;
             stats->path_per_bounce[bounce] += cnt;
             bool swapped = false;
-            trace_sort(N, T, out, out_alt, out_s2i, s2i_alt, i2s_alt, out_res, cnt, cfg->sort_path != 0,
-                       cfg->reorder_path != 0, true, smin, ssize, cfg->morton_kind, swapped);
+            const bool sort_b = cfg->sort_path != 0 && ((cfg->path_sort_skip >> bounce) & 1) == 0;
+            trace_sort(N, T, out, out_alt, out_s2i, s2i_alt, i2s_alt, out_res, cnt, sort_b,
+                       sort_b && cfg->reorder_path != 0, true, smin, ssize, cfg->morton_kind, swapped);
             orc_reconstruct_smooth(out.data(), out_res.data(), out_s2i.data(), aux.data(), dec.data(), geoms, light, bg,
                                    cnt, cfg->spp);
             if (cnt == 0) break;

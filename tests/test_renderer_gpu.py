@@ -44,7 +44,8 @@ def run_pair(wf, orc, dev, small, w, h, frames=1, **opts):
                        depth=base["recursion_depth"], radius=base["shadow_radius"], key=0.6, white=2.0, albedo=0.8,
                        sort_shadow=base["sort_shadow_rays"], reorder_shadow=base["reorder_shadow_rays"],
                        sort_path=base["sort_path_rays"], reorder_path=base["reorder_path_rays"],
-                       morton_kind=base["morton_kind"], frame_index=1)
+                       morton_kind=base["morton_kind"], frame_index=1,
+                       path_sort_skip=base.get("path_sort_skip", 0))
     o_px = None
     for f in range(1, frames + 1):
         r.render(cam, w, h, px, fp)
@@ -94,6 +95,8 @@ class same_bits:
     dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1),
     dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1, morton_kind=1,
          num_shadow_samples=3),
+    # per-bounce reordering: bounces 1 and 3 unsorted, 2 and 4 sorted + reordered
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, path_sort_skip=0b0101),
 ])
 def test_path_frame_bit_exact(wf, orc, dev, small, opts):
     px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 96, 64, **opts)

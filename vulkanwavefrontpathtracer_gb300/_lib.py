@@ -68,6 +68,7 @@ class RendererConfig(C.Structure):
         ("bvh_kind", c_int),
         ("albedo", c_float),
         ("use_graph", c_int),
+        ("path_sort_skip", c_int),
     ]
 
 

@@ -13,6 +13,8 @@ Options beyond the reference (same file, same style):
   Renderer.mortonKind     "aila32" | "6d48" | "6d64"   (default "aila32")
   Renderer.albedo         float                        (default 0.8)
   Renderer.useGraph       bool                         (default true)
+  Renderer.pathSortSkip   int bit mask: bit b set = bounce b+1 traces its
+                          path rays unsorted (per-bounce reordering, default 0)
   Benchmark.warmupCycles  int                          (default 3)
   Benchmark.benchmarkCycles int                        (default 10)
   Scene.generator         "soup:<triangles>:<seed>" | "courtyard[:<seed>]" |
@@ -65,6 +67,7 @@ DEFAULTS: Dict[str, Any] = {
     "Renderer.mortonKind": "aila32",
     "Renderer.albedo": 0.8,
     "Renderer.useGraph": True,
+    "Renderer.pathSortSkip": 0,
     "Camera.position": [0.0, 0.0, 0.0],
     "Camera.rotation": [0.0, 0.0, 0.0],
     "Camera.nearPlane": 0.001,
@@ -154,7 +157,8 @@ def renderer_config(opts: Dict[str, Any]):
         morton_kind=MORTON_KINDS[opts["Renderer.mortonKind"]],
         bvh_kind=BVH_KINDS[opts["Renderer.bvh"]],
         albedo=opts["Renderer.albedo"],
-        use_graph=1 if opts["Renderer.useGraph"] else 0)
+        use_graph=1 if opts["Renderer.useGraph"] else 0,
+        path_sort_skip=opts["Renderer.pathSortSkip"])
 
 
 # ------------------------------------------------------------ scene input

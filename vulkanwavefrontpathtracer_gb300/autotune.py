@@ -101,6 +101,41 @@ def tune_keys(scene: api.Scene, path_rays, bvh_kind: int = L.BVH8_Q8, reps: int 
     return {"best": best, "table": table}
 
 
+def tune_bounce_sort(make_renderer, camera, width: int, height: int, depth: int, frames: int = 3,
+                     device=None) -> Dict:
+    """Per-bounce reordering: greedy search of the renderer's path_sort_skip
+    mask.  make_renderer(path_sort_skip) returns a renderer with its scene
+    set (sorting and reordering of path rays on); each bounce's bit is kept
+    flipped when whole frames get faster.  Returns the best mask, its frame
+    time and the table of tried masks (median ms of `frames` frames)."""
+    import statistics
+
+    import torch
+    dev = device or torch.device("cuda", 0)
+    px = torch.zeros((width * height, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+
+    def frame_ms(mask):
+        r = make_renderer(mask)
+        r.render(camera, width, height, px, fp)  # warm-up (and graph capture)
+        times = []
+        for _ in range(frames):
+            r.render(camera, width, height, px, fp)
+            times.append(r.stats().frame_ms)
+        r.close()
+        return statistics.median(times)
+
+    best_mask, best_ms = 0, frame_ms(0)
+    table = [{"path_sort_skip": 0, "ms": best_ms}]
+    for b in range(depth):
+        mask = best_mask | (1 << b)
+        ms = frame_ms(mask)
+        table.append({"path_sort_skip": mask, "ms": ms})
+        if ms < best_ms:
+            best_mask, best_ms = mask, ms
+    return {"path_sort_skip": best_mask, "ms": best_ms, "table": table}
+
+
 def measure_work(scene: api.Scene, rays, bvh_kind: int, closest: bool) -> Dict:
     """Node visits and triangle tests per ray (counting kernel variants)."""
     import torch

@@ -417,7 +417,8 @@ struct wfpt_renderer {
                                                   out.s2i_cur(), in_res, decreases.as<float>(), out_cnt, n, in_cnt,
                                                   cfg.albedo, path_scratch.p, s)) != cudaSuccess)
                     return e;
-                if ((e = trace_rays(out, n, out_cnt, cfg.sort_path_rays != 0, cfg.reorder_path_rays != 0, true, s)) !=
+                const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
+                if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s)) !=
                     cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
@@ -448,6 +449,7 @@ wfpt_status check_config(const wfpt_renderer_config* c) {
     if (!(c->white_point > 0.0f && c->white_point <= 2.0f)) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->morton_kind < WFPT_MORTON_AILA32 || c->morton_kind > WFPT_MORTON_6D64) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->bvh_kind != WFPT_BVH2_FP32 && c->bvh_kind != WFPT_BVH8_Q8) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->path_sort_skip < 0 || c->path_sort_skip > 255) return WFPT_ERR_INVALID_ARGUMENT;
     return WFPT_OK;
 }
 
@@ -476,6 +478,7 @@ void wfpt_renderer_config_default(wfpt_renderer_config* c) {
     c->bvh_kind = WFPT_BVH2_FP32;
     c->albedo = 0.8f;
     c->use_graph = 0;
+    c->path_sort_skip = 0;
 }
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config, wfpt_renderer** renderer) {
