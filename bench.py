@@ -436,7 +436,11 @@ def run_sweep(args):
         return r
 
     bounces = autotune.tune_bounce_sort(make_renderer, cam, args.width, args.height, W["renderer"]["recursion_depth"])
-    print(json.dumps({"keys": keys, "traversal": trav, "work": work, "bounce_sort": bounces,
+    mk = torch.empty(path.shape[0], dtype=torch.int64, device=dev)
+    mi = torch.empty(path.shape[0], dtype=torch.int32, device=dev)
+    api.morton(path, scene.bounds_min, scene.bounds_max - scene.bounds_min, wf.MORTON_6D64, mk, mi)
+    sort = autotune.tune_sort(mk, 63)
+    print(json.dumps({"keys": keys, "traversal": trav, "work": work, "bounce_sort": bounces, "sort": sort,
                       "resolution": [args.width, args.height]}))
 
 

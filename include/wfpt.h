@@ -130,6 +130,7 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          (equally valid) occluder
  *   "sort.tiles"           radix sort tile size: 0 = by problem size
  *                          (default), 1 = small tiles, 2 = large tiles
+ *   "sort.digit_bits"      radix digit width per pass: 8 (default) or 4
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */

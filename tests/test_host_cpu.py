@@ -282,7 +282,7 @@ def test_tuning_knobs(wf):
         assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
         assert api.tune_get("trace.bvh8.coop") == 0
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
-                         ("trace.bvh8.coop", 2), ("sort.tiles", 3), ("sort.tiles", -1), ("no.such.knob", 1)):
+                         ("trace.bvh8.coop", 2), ("sort.tiles", 3), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("no.such.knob", 1)):
             with pytest.raises(wf.WfptError):
                 api.tune_set(key, bad)
     finally:

@@ -121,24 +121,31 @@ def test_sort_scratch_too_small(wf, dev):
         wf.api.sort_pairs(k, v, 32, scratch=small)
 
 
+@pytest.mark.parametrize("digit_bits", [8, 4])
 @pytest.mark.parametrize("tiles", [1, 2])
-@pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4097, 32), (123457, 32),
-                                        (1535, 63), (1537, 64), (3073, 63), (300001, 48), (2073600, 63)])
-def test_sort_tile_variants(wf, dev, tiles, n, key_bits):
-    """Both tile sizes give the stable order, at sizes around both tile
-    boundaries, including the frame's wavefront size."""
+@pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4097, 32), (123457, 32), (9000, 12),
+                                        (70001, 33), (1535, 63), (1537, 64), (3073, 63), (300001, 48),
+                                        (65537, 62), (2073600, 63)])
+def test_sort_tile_variants(wf, dev, tiles, n, key_bits, digit_bits):
+    """Both tile sizes and both digit widths give the stable order, at sizes
+    around the tile boundaries, odd and even pass counts, key widths that
+    are not multiples of the digit width, and the frame's wavefront size."""
     rng = np.random.default_rng(n + key_bits)
     if key_bits > 32:
         keys = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
     else:
         keys = rng.integers(0, 2**32, n, dtype=np.uint32)
     keys[::5] = keys[len(keys) // 2]  # duplicates: stability matters
-    old = wf.api.tune_get("sort.tiles")
+    if key_bits < 32:
+        keys &= np.uint32((1 << key_bits) - 1) | np.uint32(0xF0000000)  # high bits outside key_bits are ignored
+    old = wf.api.tune_get("sort.tiles"), wf.api.tune_get("sort.digit_bits")
     try:
         wf.api.tune_set("sort.tiles", tiles)
+        wf.api.tune_set("sort.digit_bits", digit_bits)
         k, v = run_sort(wf, dev, keys, key_bits)
     finally:
-        wf.api.tune_set("sort.tiles", old)
+        wf.api.tune_set("sort.tiles", old[0])
+        wf.api.tune_set("sort.digit_bits", old[1])
     rk, rv = stable_ref(keys, key_bits)
     assert np.array_equal(v, rv) and np.array_equal(k, rk)
     assert wf.api.device_status() == 0

@@ -101,6 +101,37 @@ def tune_keys(scene: api.Scene, path_rays, bvh_kind: int = L.BVH8_Q8, reps: int 
     return {"best": best, "table": table}
 
 
+def tune_sort(keys, key_bits: int, reps: int = 10) -> Dict:
+    """Radix digit width (4 or 8 bits) x tile variant (small, large) for
+    sorts of `keys` (a device tensor of int32 / int64 keys); returns the
+    fastest setting and the table (ms per sort, keys restored before
+    every sort)."""
+    import torch
+    n = keys.shape[0]
+    work = keys.clone()
+    vals = torch.empty(n, dtype=torch.int32, device=keys.device)
+    scratch = torch.empty(api.sort_scratch_bytes(n, 64 if key_bits > 32 else 32), dtype=torch.uint8,
+                          device=keys.device)
+    old = (api.tune_get("sort.digit_bits"), api.tune_get("sort.tiles"))
+    table = []
+    try:
+        for db, tiles in itertools.product((8, 4), (1, 2)):
+            api.tune_set("sort.digit_bits", db)
+            api.tune_set("sort.tiles", tiles)
+
+            def one():
+                work.copy_(keys)
+                api.sort_pairs(work, vals, key_bits, scratch=scratch)
+
+            copy_ms = _timeit(lambda: work.copy_(keys), reps)
+            table.append({"digit_bits": db, "tiles": tiles, "ms": max(_timeit(one, reps) - copy_ms, 0.0)})
+    finally:
+        api.tune_set("sort.digit_bits", old[0])
+        api.tune_set("sort.tiles", old[1])
+    best = min(table, key=lambda e: e["ms"])
+    return {"digit_bits": best["digit_bits"], "tiles": best["tiles"], "table": table}
+
+
 def tune_bounce_sort(make_renderer, camera, width: int, height: int, depth: int, frames: int = 3,
                      device=None) -> Dict:
     """Per-bounce reordering: greedy search of the renderer's path_sort_skip

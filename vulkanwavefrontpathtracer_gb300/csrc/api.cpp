@@ -106,6 +106,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_sort_tiles((int)value);
         return WFPT_OK;
     }
+    if (k == "sort.digit_bits") {
+        if (value != 4 && value != 8) return invalid("sort.digit_bits must be 4 or 8");
+        wfpt::set_sort_digit_bits((int)value);
+        return WFPT_OK;
+    }
     if (k == "trace.count") {
         if (value < 0 || value > 1) return invalid("trace.count must be 0 or 1");
         wfpt::set_trace_count(value != 0);
@@ -138,6 +143,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "sort.tiles") {
         *value = wfpt::get_sort_tiles();
+        return WFPT_OK;
+    }
+    if (k == "sort.digit_bits") {
+        *value = wfpt::get_sort_digit_bits();
         return WFPT_OK;
     }
     if (k == "trace.count") {

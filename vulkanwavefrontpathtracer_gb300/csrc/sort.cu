@@ -42,10 +42,11 @@ constexpr int kLbChunk = 16;  // predecessors read per look-back round trip
 constexpr int kKptSmall32 = 8, kKptLarge32 = 16;
 constexpr int kKptSmall64 = 8, kKptLarge64 = 14;
 
-// Digit mask of pass p: the top pass keeps only the bits below key_bits.
-__host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p) {
-    int bits = key_bits - 8 * p;
-    return bits >= 8 ? 0xFFu : ((1u << bits) - 1u);
+// Digit mask of pass p with db-bit digits: the top pass keeps only the
+// bits below key_bits.
+__host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p, int db = 8) {
+    int bits = key_bits - db * p;
+    return bits >= db ? ((1u << db) - 1u) : ((1u << bits) - 1u);
 }
 __device__ __forceinline__ uint32_t digit_of(uint32_t k, int shift, uint32_t dmask) { return (k >> shift) & dmask; }
 __device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift, uint32_t dmask) { return (uint32_t)(k >> shift) & dmask; }
@@ -136,10 +137,13 @@ static void launch_hist(const K* keys, uint32_t n, const uint32_t* n_dev, int pa
     }
 }
 
-// One digit pass.  Dynamic shared memory: TILE keys, TILE values,
-// kSortWarps*256 per-warp digit counters, 256 global bases, 256 local
-// offsets.
-template <typename K, int KPT>
+// One digit pass with DB-bit digits (RADIX = 2^DB bins).  Dynamic shared
+// memory: TILE keys, TILE values, kSortWarps*RADIX per-warp digit
+// counters, RADIX global bases, RADIX local offsets.  hist is the byte
+// histogram (k_sort_hist) of this pass's byte; with 4-bit digits a digit's
+// count is the sum of the 16 byte bins sharing that nibble (nibble 0: low
+// nibble of the byte, 1: high nibble).
+template <typename K, int KPT, int DB>
 __global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               K* __restrict__ keys_out,
@@ -147,8 +151,9 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restric
                                                               const uint32_t* __restrict__ n_dev, int shift,
                                                               uint32_t dmask, const uint32_t* __restrict__ hist,
                                                               uint32_t* __restrict__ lookback,
-                                                              uint32_t* __restrict__ ticket) {
+                                                              uint32_t* __restrict__ ticket, int nibble) {
     constexpr uint32_t TILE = kSortThreads * KPT;
+    constexpr int kRadix = 1 << DB;
     extern __shared__ __align__(16) unsigned char smem[];
     K* s_keys = reinterpret_cast<K*>(smem);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restric
         uint32_t d = digit_of(key[k], shift, dmask);
         uint32_t peers = __ballot_sync(0xffffffffu, ok);
 #pragma unroll
-        for (int b = 0; b < 8; ++b) {
+        for (int b = 0; b < DB; ++b) {
             uint32_t bit = (d >> b) & 1u;
             uint32_t m = __ballot_sync(0xffffffffu, bit);
             peers &= bit ? m : ~m;
@@ -199,8 +204,8 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restric
     }
     __syncthreads();
 
-    // Threads 0..255 own one digit each: warp-exclusive prefixes and the
-    // tile's count of that digit.
+    // Threads 0..RADIX-1 own one digit each: warp-exclusive prefixes and
+    // the tile's count of that digit.
     const bool owner = threadIdx.x < kRadix;
     const uint32_t d = threadIdx.x & (kRadix - 1);
     uint32_t run = 0;
@@ -218,8 +223,16 @@ __global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restric
     // global histogram) before staging, so that successors can proceed.
     uint32_t excl = 0;
     if (tile == 0) {
-        uint32_t total;
-        excl = block_exclusive_scan<kSortWarps>(owner ? hist[d] : 0u, s_scan, &total);
+        uint32_t total, cnt_d = 0;
+        if (owner) {
+            if (DB == 8) {
+                cnt_d = hist[d];
+            } else {
+#pragma unroll
+                for (uint32_t j = 0; j < 16; ++j) cnt_d += hist[nibble ? ((d << 4) | j) : ((j << 4) | d)];
+            }
+        }
+        excl = block_exclusive_scan<kSortWarps>(cnt_d, s_scan, &total);
     }
     uint32_t* lb = lookback + (size_t)tile * kRadix + d;
     if (owner) {
@@ -305,9 +318,15 @@ __global__ void k_copy_back(const K* __restrict__ ks, const uint32_t* __restrict
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-template <typename K, int KPT>
+template <typename K, int KPT, int DB>
 static size_t onesweep_smem() {
-    return (size_t)kSortThreads * KPT * (sizeof(K) + 4) + (size_t)(kSortWarps + 2) * kRadix * 4;
+    return (size_t)kSortThreads * KPT * (sizeof(K) + 4) + (size_t)(kSortWarps + 2) * (1u << DB) * 4;
+}
+
+template <typename K, int KPT, int DB>
+static cudaError_t opt_in_smem() {
+    return cudaFuncSetAttribute(k_onesweep<K, KPT, DB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)onesweep_smem<K, KPT, DB>());
 }
 
 static int g_num_sms = 0;
@@ -317,19 +336,14 @@ static int g_num_sms = 0;
 // renderer calls this before capturing a frame graph).
 cudaError_t sort_prepare() {
     if (g_num_sms != 0) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_onesweep<uint32_t, kKptSmall32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)onesweep_smem<uint32_t, kKptSmall32>());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_onesweep<uint32_t, kKptLarge32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)onesweep_smem<uint32_t, kKptLarge32>());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_onesweep<uint64_t, kKptSmall64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)onesweep_smem<uint64_t, kKptSmall64>());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_onesweep<uint64_t, kKptLarge64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)onesweep_smem<uint64_t, kKptLarge64>());
+    cudaError_t e = opt_in_smem<uint32_t, kKptSmall32, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptLarge32, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptSmall64, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptLarge64, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptSmall32, 4>();
+    if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptLarge32, 4>();
+    if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptSmall64, 4>();
+    if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptLarge64, 4>();
     int dev = 0, sms = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -343,6 +357,12 @@ cudaError_t sort_prepare() {
 static int g_sort_tiles = 0;
 void set_sort_tiles(int v) { g_sort_tiles = v < 0 ? 0 : (v > 2 ? 2 : v); }
 int get_sort_tiles() { return g_sort_tiles; }
+
+// Digit width: 8 (default) or 4 bits per pass (twice the passes, 16-bin
+// ranking).
+static int g_digit_bits = 8;
+void set_sort_digit_bits(int v) { g_digit_bits = v == 4 ? 4 : 8; }
+int get_sort_digit_bits() { return g_digit_bits; }
 
 static bool use_large_tiles(uint32_t n, bool wide) {
     if (g_sort_tiles != 0) return g_sort_tiles == 2;
@@ -377,32 +397,38 @@ size_t sort_scratch_bytes(uint32_t max_n, int key_bits) {
     return sort_layout(max_n, key_bits).total;
 }
 
-template <typename K, int KPT>
+// The layout is sized for 8-bit digits; 4-bit digits take at most twice the
+// passes with 1/16 of the look-back entries per pass, and their global digit
+// counts come from the same byte histograms.
+template <typename K, int KPT, int DB>
 static cudaError_t sort_passes(K* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
                                const SortLayout& L, unsigned char* scratch, cudaStream_t s) {
     constexpr uint32_t TILE = kSortThreads * KPT;
+    constexpr uint32_t RADIX = 1u << DB;
+    const int passes = (key_bits + DB - 1) / DB;
     uint32_t* tickets = reinterpret_cast<uint32_t*>(scratch + L.off_ticket);
     uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + L.off_hist);
     uint32_t* lookback = reinterpret_cast<uint32_t*>(scratch + L.off_lookback);
     K* alt_keys = reinterpret_cast<K*>(scratch + L.off_keys);
     uint32_t* alt_vals = reinterpret_cast<uint32_t*>(scratch + L.off_vals);
     const uint32_t tiles = (n + TILE - 1) / TILE;
-    const size_t smem = onesweep_smem<K, KPT>();
+    const size_t smem = onesweep_smem<K, KPT, DB>();
     cudaError_t e;
     K* src_k = keys;
     uint32_t* src_v = values;
     K* dst_k = alt_keys;
     uint32_t* dst_v = alt_vals;
-    for (int p = 0; p < L.passes; ++p) {
-        k_onesweep<K, KPT><<<tiles, kSortThreads, smem, s>>>(src_k, src_v, dst_k, dst_v, n, n_dev, 8 * p,
-                                                             pass_mask(key_bits, p), hist + p * kRadix,
-                                                             lookback + (size_t)p * L.tiles * kRadix, tickets + p);
+    for (int p = 0; p < passes; ++p) {
+        const int byte = DB == 8 ? p : p / 2;
+        k_onesweep<K, KPT, DB><<<tiles, kSortThreads, smem, s>>>(
+            src_k, src_v, dst_k, dst_v, n, n_dev, DB * p, pass_mask(key_bits, p, DB), hist + byte * kRadix,
+            lookback + (size_t)p * L.tiles * RADIX, tickets + p, DB == 8 ? 0 : (p & 1));
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(src_k, dst_k);
         std::swap(src_v, dst_v);
     }
-    if (L.passes & 1) {
+    if (passes & 1) {
         unsigned cgrid = (unsigned)std::min<size_t>(((size_t)n + 255) / 256, 152 * 16);
         k_copy_back<K><<<cgrid, 256, 0, s>>>(alt_keys, alt_vals, keys, values, n, n_dev);
         count_launch();
@@ -427,9 +453,13 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     constexpr bool wide = sizeof(K) == 8;
-    if (use_large_tiles(n, wide))
-        return sort_passes<K, wide ? kKptLarge64 : kKptLarge32>(keys, values, n, n_dev, key_bits, L, scratch, s);
-    return sort_passes<K, wide ? kKptSmall64 : kKptSmall32>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    constexpr int large = wide ? kKptLarge64 : kKptLarge32, small = wide ? kKptSmall64 : kKptSmall32;
+    const bool lt = use_large_tiles(n, wide);
+    if (g_digit_bits == 4)
+        return lt ? sort_passes<K, large, 4>(keys, values, n, n_dev, key_bits, L, scratch, s)
+                  : sort_passes<K, small, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    return lt ? sort_passes<K, large, 8>(keys, values, n, n_dev, key_bits, L, scratch, s)
+              : sort_passes<K, small, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
 }
 
 cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,

@@ -79,6 +79,9 @@ size_t sort_scratch_bytes(uint32_t max_n, int key_bits);
 // Sort tile variant: 0 = automatic by size, 1 = small tiles, 2 = large tiles.
 void set_sort_tiles(int v);
 int get_sort_tiles();
+// Radix digit width: 8 (default) or 4 bits per pass.
+void set_sort_digit_bits(int v);
+int get_sort_digit_bits();
 cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev,
                               int key_bits, void* scratch, size_t scratch_bytes, cudaStream_t s);
 
