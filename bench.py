@@ -748,7 +748,16 @@ def run_sort_micro(args):
         ms = timeit(lambda: api.reorder(perm, rays, out, s2i, os2i, oi2s), reps)
         rows.append({"n": n, "reorder_ms": round(ms, 4), "reorder_gbs": round(80.0 * n / (ms * 1e-3) / 1e9, 1),
                      "reorder_frac": round(80.0 * n / (ms * 1e-3) / 1e9 / hbm, 3)})
-        del rays, keys, ids, scratch, out
+        # The same gather of 48-byte records (the ray plus a 16-byte
+        # payload) with the slot maps: 4 + 4 + 48 B read, 48 + 4 + 4 B
+        # written per ray.
+        wide = torch.cat([rays, rays[:, :4]], dim=1).contiguous()
+        wide_out = torch.empty_like(wide)
+        del out
+        ms = timeit(lambda: api.reorder_records(perm, wide, wide_out, s2i, os2i, oi2s), reps)
+        rows.append({"n": n, "reorder48_ms": round(ms, 4), "reorder48_gbs": round(112.0 * n / (ms * 1e-3) / 1e9, 1),
+                     "reorder48_frac": round(112.0 * n / (ms * 1e-3) / 1e9 / hbm, 3)})
+        del rays, keys, ids, scratch, wide, wide_out
         torch.cuda.empty_cache()
     print(json.dumps({"sort_micro": rows, "peak_gbs": hbm, "peak_source": f"{peak_kind} hbm_gbs",
                       "sort_tiles": api.tune_get("sort.tiles")}))

@@ -129,7 +129,9 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          identical; an any-hit ray may report a different
  *                          (equally valid) occluder
  *   "sort.tiles"           radix sort tile size: 0 = by problem size
- *                          (default), 1 = small tiles, 2 = large tiles
+ *                          (default), 1 = small tiles, 2 = large tiles,
+ *                          3 = extra-large tiles (32-bit keys; 64-bit keys
+ *                          take the large ones)
  *   "sort.digit_bits"      radix digit width per pass: 8 (default) or 4
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
@@ -207,6 +209,19 @@ wfpt_status wfpt_reorder(const uint32_t* ray_index, const wfpt_ray* in_rays,
                          wfpt_ray* out_rays, const int32_t* in_slot_to_index,
                          int32_t* out_slot_to_index, int32_t* out_index_to_slot,
                          uint32_t n, const uint32_t* n_dev, void* stream);
+
+/* The reorder gather for records other than the 32-byte wfpt_ray (ray
+ * records carrying a payload; 48 B is the wide layout the sort/reorder
+ * microbenchmark uses).  No reference counterpart: reorderRays.comp:37-45
+ * moves 32-byte Ray records only.  out_records[i] = in_records[ray_index[i]]
+ * for records of record_bytes = 16, 32, 48 or 64 bytes; both record buffers
+ * 16-byte aligned.  The slot maps follow wfpt_reorder when given; pass all
+ * three as NULL for a plain gather. */
+wfpt_status wfpt_reorder_records(const uint32_t* ray_index, const void* in_records,
+                                 void* out_records, uint32_t record_bytes,
+                                 const int32_t* in_slot_to_index,
+                                 int32_t* out_slot_to_index, int32_t* out_index_to_slot,
+                                 uint32_t n, const uint32_t* n_dev, void* stream);
 
 /* raygenShadow.comp:68-137 + RayGen::shadow (RayGen.cpp:107-133).  Seeds
  * are indexed by batch-local task index like the reference. */

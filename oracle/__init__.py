@@ -131,6 +131,21 @@ def reorder(idx, in_rays, in_s2i, index_space=None):
     return out, s2i, i2s
 
 
+def reorder_records(idx, in_records, in_s2i=None, index_space=None):
+    """Gather of fixed-width records (rows of `in_records`, any dtype) by
+    `idx`; slot maps as in reorder() when in_s2i is given."""
+    n = idx.shape[0]
+    src = np.ascontiguousarray(in_records)
+    rb = src.shape[1] * src.itemsize
+    out = np.empty((n,) + src.shape[1:], src.dtype)
+    s2i = np.empty(n, np.int32) if in_s2i is not None else None
+    i2s = np.full(index_space or n, -1, np.int32) if in_s2i is not None else None
+    _call(load().orc_reorder_records, ptr(np.ascontiguousarray(idx, np.uint32)), ptr(src), ptr(out), C.c_uint32(rb),
+          ptr(np.ascontiguousarray(in_s2i, np.int32)) if in_s2i is not None else None, ptr(s2i) if s2i is not None
+          else None, ptr(i2s) if i2s is not None else None, C.c_uint32(n))
+    return out, s2i, i2s
+
+
 def sobol2d(i):
     x, y = C.c_float(), C.c_float()
     _call(load().orc_sobol2d, C.c_uint32(i), C.byref(x), C.byref(y))

@@ -318,6 +318,21 @@ extern "C" void orc_reorder(const uint32_t* idx, const ORay* in_rays, ORay* out_
     }
 }
 
+// The same gather for records of any width (the 48-byte wide-record layout
+// of the sort/reorder microbenchmark); slot maps optional (in_s2i null).
+extern "C" void orc_reorder_records(const uint32_t* idx, const uint8_t* in_rec, uint8_t* out_rec, uint32_t record_bytes,
+                                    const int32_t* in_s2i, int32_t* out_s2i, int32_t* out_i2s, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t old = idx[i];
+        std::memcpy(out_rec + (size_t)i * record_bytes, in_rec + (size_t)old * record_bytes, record_bytes);
+        if (in_s2i) {
+            int32_t index = in_s2i[old];
+            out_s2i[i] = index;
+            out_i2s[index] = (int32_t)i;
+        }
+    }
+}
+
 // ---------------------------------------------------------- raygenShadow
 // raygenShadow.comp:10-44 and :82-136.
 static void jenkins(uint32_t& a, uint32_t& b, uint32_t& c) {

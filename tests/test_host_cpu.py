@@ -46,6 +46,13 @@ def test_invalid_arguments_rejected_on_host(wf):
     assert lib.wfpt_morton(None, 5, None, wf._lib.fvec([0, 0, 0]), wf._lib.fvec([1, 1, 1]), 0, None, None, None) == 1
     assert lib.wfpt_morton(buf, 5, None, wf._lib.fvec([0, 0, 0]), wf._lib.fvec([1, 1, 1]), 7, buf, buf, None) == 1
     assert lib.wfpt_reorder(buf, buf, buf, buf, buf, buf, 4, None, None) == 1  # in place
+    other = C.c_void_p(0x2000)
+    assert lib.wfpt_reorder_records(buf, buf, other, 40, None, None, None, 4, None, None) == 1  # width
+    assert lib.wfpt_reorder_records(buf, buf, other, 48, buf, None, None, 4, None, None) == 1  # partial maps
+    assert lib.wfpt_reorder_records(buf, C.c_void_p(0x1008), other, 48, None, None, None, 4, None, None) == 1
+    assert b"aligned" in lib.wfpt_last_error_message()
+    assert lib.wfpt_reorder_records(buf, buf, buf, 48, None, None, None, 4, None, None) == 1  # in place
+    assert lib.wfpt_reorder_records(None, None, None, 48, None, None, None, 0, None, None) == 0  # empty
     assert lib.wfpt_raygen_shadow(buf, buf, buf, buf, buf, buf, wf._lib.fvec([0, 0, 0]), 1.0, 0, 4, None, 0,
                                   None) == 1
     assert lib.wfpt_trace(None, 0, buf, buf, None, 4, None, 1, None) == 1
@@ -282,7 +289,7 @@ def test_tuning_knobs(wf):
         assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
         assert api.tune_get("trace.bvh8.coop") == 0
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
-                         ("trace.bvh8.coop", 2), ("sort.tiles", 3), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("no.such.knob", 1)):
+                         ("trace.bvh8.coop", 2), ("sort.tiles", 4), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("no.such.knob", 1)):
             with pytest.raises(wf.WfptError):
                 api.tune_set(key, bad)
     finally:

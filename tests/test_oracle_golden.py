@@ -78,6 +78,25 @@ def test_sort_is_stable(orc):
     assert np.array_equal(v2, order.astype(np.uint32))
 
 
+def test_reorder_records_matches_reorder(orc):
+    # The wide-record gather is the 32-byte reorder at record_bytes 32, and a
+    # plain row gather (with the same slot maps) at 48.
+    rng = np.random.default_rng(5)
+    n = 1000
+    idx = rng.permutation(n).astype(np.uint32)
+    s2i = rng.permutation(n).astype(np.int32)
+    rays = rng.standard_normal((n, 8)).astype(np.float32)
+    a, a_s2i, a_i2s = orc.reorder(idx, rays, s2i)
+    b, b_s2i, b_i2s = orc.reorder_records(idx, rays, s2i)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(a_s2i, b_s2i) and np.array_equal(a_i2s, b_i2s)
+    wide = rng.integers(0, 2**32, size=(n, 12), dtype=np.uint32)
+    c, c_s2i, c_i2s = orc.reorder_records(idx, wide, s2i)
+    assert np.array_equal(c, wide[idx]) and np.array_equal(c_s2i, a_s2i) and np.array_equal(c_i2s, a_i2s)
+    d, d_s2i, _ = orc.reorder_records(idx, wide)
+    assert np.array_equal(d, wide[idx]) and d_s2i is None
+
+
 def test_reinhard(orc):
     for c, key, white, expect in GOLDEN["reinhard"]:
         fp = np.array([[*c, 1.0]], np.float32)

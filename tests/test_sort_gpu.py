@@ -122,12 +122,13 @@ def test_sort_scratch_too_small(wf, dev):
 
 
 @pytest.mark.parametrize("digit_bits", [8, 4])
-@pytest.mark.parametrize("tiles", [1, 2])
-@pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4097, 32), (123457, 32), (9000, 12),
-                                        (70001, 33), (1535, 63), (1537, 64), (3073, 63), (300001, 48),
-                                        (65537, 62), (2073600, 63)])
+@pytest.mark.parametrize("tiles", [1, 2, 3])
+@pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4095, 32), (4097, 32), (8191, 32),
+                                        (8193, 32), (10239, 32), (10241, 32), (123457, 32), (9000, 12),
+                                        (70001, 33), (1535, 63), (1537, 64), (3073, 63), (7167, 63), (7169, 63),
+                                        (14337, 64), (300001, 48), (65537, 62), (2073600, 63)])
 def test_sort_tile_variants(wf, dev, tiles, n, key_bits, digit_bits):
-    """Both tile sizes and both digit widths give the stable order, at sizes
+    """Every tile size and both digit widths give the stable order, at sizes
     around the tile boundaries, odd and even pass counts, key widths that
     are not multiples of the digit width, and the frame's wavefront size."""
     rng = np.random.default_rng(n + key_bits)

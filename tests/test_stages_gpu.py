@@ -86,6 +86,36 @@ def test_reorder(wf, orc, dev):
     assert np.array_equal(N(os2i), r_s2i) and np.array_equal(N(oi2s), r_i2s)
 
 
+@pytest.mark.parametrize("words,maps,counted", [(12, True, False), (12, False, True), (4, True, False),
+                                                (8, True, True), (16, False, False)])
+def test_reorder_records(wf, orc, dev, words, maps, counted):
+    # 48-byte (12-word) wide records, and the 16/32/64-byte widths, with and
+    # without slot maps; `counted` reads n from device memory.
+    import torch
+    rng = np.random.default_rng(words * 7 + maps)
+    n = 50003
+    recs = rng.integers(0, 2**32, size=(n, words), dtype=np.uint32).view(np.int32)
+    perm = rng.permutation(n).astype(np.uint32)
+    s2i = rng.permutation(n).astype(np.int32)
+    out = torch.full((n, words), -7, dtype=torch.int32, device=dev)
+    os2i = torch.empty(n, dtype=torch.int32, device=dev) if maps else None
+    oi2s = torch.empty(n, dtype=torch.int32, device=dev) if maps else None
+    m = n - 1000 if counted else n
+    n_dev = torch.tensor([m], dtype=torch.int32, device=dev) if counted else None
+    wf.api.reorder_records(T(perm.view(np.int32), dev), T(recs, dev), out, T(s2i, dev) if maps else None, os2i,
+                           oi2s, n=n, n_dev=n_dev)
+    if counted:
+        # only the first m slots are written; the rest keep their fill
+        ref = recs[perm[:m]]
+        got = N(out)
+        assert np.array_equal(got[:m], ref) and np.all(got[m:] == -7)
+        return
+    r_out, r_s2i, r_i2s = orc.reorder_records(perm, recs, s2i if maps else None)
+    assert np.array_equal(N(out), r_out)
+    if maps:
+        assert np.array_equal(N(os2i), r_s2i) and np.array_equal(N(oi2s), r_i2s)
+
+
 def _hits_for(rays, rng, miss_frac=0.3):
     n = rays.shape[0]
     res = np.zeros((n, 4), np.int32)

@@ -121,6 +121,20 @@ def reorder(ray_index, in_rays, out_rays, in_slot_to_index, out_slot_to_index, o
                                _p(out_index_to_slot), _n(ray_index, n), _p(n_dev), _s(stream)))
 
 
+def reorder_records(ray_index, in_records, out_records, in_slot_to_index=None, out_slot_to_index=None,
+                    out_index_to_slot=None, n=None, n_dev=None, stream=None):
+    """Reorder gather of fixed-width records (rows of 16, 32, 48 or 64
+    bytes); the slot maps are optional, as in wfpt_reorder_records."""
+    if in_records.dim() != 2 or not in_records.is_contiguous() or not out_records.is_contiguous():
+        raise ValueError("records are the rows of a contiguous 2-D tensor")
+    rb = in_records.stride(0) * in_records.element_size()
+    if out_records.dim() != 2 or out_records.stride(0) * out_records.element_size() != rb:
+        raise ValueError("in_records and out_records rows differ in width")
+    L.check(lib().wfpt_reorder_records(_p(ray_index), _p(in_records), _p(out_records), rb, _p(in_slot_to_index),
+                                       _p(out_slot_to_index), _p(out_index_to_slot), _n(ray_index, n), _p(n_dev),
+                                       _s(stream)))
+
+
 def trace(scene: "Scene", bvh_kind, rays, results, ray_index=None, closest_hit=True, n=None, n_dev=None,
           stream=None):
     L.check(lib().wfpt_trace(scene.handle, bvh_kind, _p(rays), _p(results), _p(ray_index), _n(rays, n), _p(n_dev),

@@ -102,7 +102,8 @@ def tune_keys(scene: api.Scene, path_rays, bvh_kind: int = L.BVH8_Q8, reps: int 
 
 
 def tune_sort(keys, key_bits: int, reps: int = 10) -> Dict:
-    """Radix digit width (4 or 8 bits) x tile variant (small, large) for
+    """Radix digit width (4 or 8 bits) x tile variant (small, large,
+    extra-large; 64-bit keys have no extra-large tile, so 3 repeats 2) for
     sorts of `keys` (a device tensor of int32 / int64 keys); returns the
     fastest setting and the table (ms per sort, keys restored before
     every sort)."""
@@ -115,7 +116,7 @@ def tune_sort(keys, key_bits: int, reps: int = 10) -> Dict:
     old = (api.tune_get("sort.digit_bits"), api.tune_get("sort.tiles"))
     table = []
     try:
-        for db, tiles in itertools.product((8, 4), (1, 2)):
+        for db, tiles in itertools.product((8, 4), (1, 2) if key_bits > 32 else (1, 2, 3)):
             api.tune_set("sort.digit_bits", db)
             api.tune_set("sort.tiles", tiles)
 

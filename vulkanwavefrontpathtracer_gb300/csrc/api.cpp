@@ -102,7 +102,8 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         return WFPT_OK;
     }
     if (k == "sort.tiles") {
-        if (value < 0 || value > 2) return invalid("sort.tiles must be 0 (auto), 1 (small) or 2 (large)");
+        if (value < 0 || value > 3)
+            return invalid("sort.tiles must be 0 (auto), 1 (small), 2 (large) or 3 (extra-large)");
         wfpt::set_sort_tiles((int)value);
         return WFPT_OK;
     }
@@ -254,6 +255,24 @@ wfpt_status wfpt_reorder(const uint32_t* ray_index, const wfpt_ray* in_rays, wfp
     WFPT_REQUIRE(n == 0 || (const void*)in_rays != (const void*)out_rays, "reorder cannot run in place");
     return from_cuda(wfpt::launch_reorder(ray_index, in_rays, out_rays, in_slot_to_index, out_slot_to_index,
                                           out_index_to_slot, n, n_dev, S(stream)));
+}
+
+wfpt_status wfpt_reorder_records(const uint32_t* ray_index, const void* in_records, void* out_records,
+                                 uint32_t record_bytes, const int32_t* in_slot_to_index, int32_t* out_slot_to_index,
+                                 int32_t* out_index_to_slot, uint32_t n, const uint32_t* n_dev, void* stream) {
+    WFPT_REQUIRE(n <= kMaxN, "n too large");
+    WFPT_REQUIRE(record_bytes == 16 || record_bytes == 32 || record_bytes == 48 || record_bytes == 64,
+                 "record_bytes must be 16, 32, 48 or 64");
+    const bool maps = in_slot_to_index || out_slot_to_index || out_index_to_slot;
+    WFPT_REQUIRE(!maps || (in_slot_to_index && out_slot_to_index && out_index_to_slot),
+                 "slot maps: pass all three or none");
+    WFPT_REQUIRE(n == 0 || (ray_index && in_records && out_records), "null buffer");
+    WFPT_REQUIRE(n == 0 || ((reinterpret_cast<uintptr_t>(in_records) | reinterpret_cast<uintptr_t>(out_records)) &
+                            15u) == 0,
+                 "record buffers must be 16-byte aligned");
+    WFPT_REQUIRE(n == 0 || in_records != (const void*)out_records, "reorder cannot run in place");
+    return from_cuda(wfpt::launch_reorder_records(ray_index, in_records, out_records, record_bytes, in_slot_to_index,
+                                                  out_slot_to_index, out_index_to_slot, n, n_dev, S(stream)));
 }
 
 wfpt_status wfpt_raygen_shadow(const uint32_t* seeds, const wfpt_ray* in_rays, const wfpt_hit* in_results,

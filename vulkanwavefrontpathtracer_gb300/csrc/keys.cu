@@ -118,6 +118,30 @@ __global__ void k_reorder(const uint32_t* __restrict__ idx, const float4* __rest
     out_i2s[index] = (int32_t)i;
 }
 
+// The same gather for records of C x 16 bytes (ray records with a payload,
+// 48 B = 3 chunks).  One thread per record: the C 16-byte loads of a record
+// are issued together; stores are coalesced across the warp.  The slot maps
+// are optional (in_s2i == nullptr: plain gather).
+template <int C>
+__global__ void k_reorder_records(const uint32_t* __restrict__ idx, const uint4* __restrict__ in_rec,
+                                  uint4* __restrict__ out_rec, const int32_t* __restrict__ in_s2i,
+                                  int32_t* __restrict__ out_s2i, int32_t* __restrict__ out_i2s, uint32_t n,
+                                  const uint32_t* __restrict__ n_dev) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= load_count(n, n_dev)) return;
+    uint32_t old = idx[i];
+    uint4 v[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) v[c] = __ldg(in_rec + (size_t)C * old + c);
+#pragma unroll
+    for (int c = 0; c < C; ++c) out_rec[(size_t)C * i + c] = v[c];
+    if (in_s2i != nullptr) {
+        int32_t index = in_s2i[old];
+        out_s2i[i] = index;
+        out_i2s[index] = (int32_t)i;
+    }
+}
+
 cudaError_t launch_morton(const wfpt_ray* rays, uint32_t n, const uint32_t* n_dev, const float* smin,
                           const float* ssize, int kind, void* keys, uint32_t* indices, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
@@ -144,6 +168,24 @@ cudaError_t launch_reorder(const uint32_t* idx, const wfpt_ray* in_rays, wfpt_ra
     unsigned grid = (n + kBlock - 1) / kBlock;
     k_reorder<<<grid, kBlock, 0, s>>>(idx, reinterpret_cast<const float4*>(in_rays),
                                       reinterpret_cast<float4*>(out_rays), in_s2i, out_s2i, out_i2s, n, n_dev);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reorder_records(const uint32_t* idx, const void* in_records, void* out_records,
+                                   uint32_t record_bytes, const int32_t* in_s2i, int32_t* out_s2i, int32_t* out_i2s,
+                                   uint32_t n, const uint32_t* n_dev, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    unsigned grid = (n + kBlock - 1) / kBlock;
+    const uint4* in = static_cast<const uint4*>(in_records);
+    uint4* out = static_cast<uint4*>(out_records);
+    switch (record_bytes) {
+        case 16: k_reorder_records<1><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
+        case 32: k_reorder_records<2><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
+        case 48: k_reorder_records<3><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
+        case 64: k_reorder_records<4><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
+        default: return cudaErrorInvalidValue;
+    }
     count_launch();
     return cudaGetLastError();
 }

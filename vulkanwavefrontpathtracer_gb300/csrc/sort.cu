@@ -5,7 +5,7 @@
 // with a single-sweep scheme after Adinets & Merrill ("Onesweep", 2022):
 //   1. one histogram kernel reads the keys once and builds the 256-bin digit
 //      histogram of every pass (the global digit bases);
-//   2. per pass, one kernel of 1024-thread CTAs, one CTA per SM: each takes
+//   2. per pass, one kernel of 512-thread CTAs, two resident per SM: each takes
 //      the next tile from a ticket counter, ranks its keys with warp ballots
 //      (stable: keys are ranked in input order), publishes its per-digit
 //      counts, stages the tile in shared memory in digit order, resolves the
@@ -13,9 +13,9 @@
 //      tiles and writes keys and values out in coalesced runs.
 // Sized for a frame's wavefronts (a few million keys, all of it resident in
 // L2): tiles of 8 or 14-16 keys per thread make such a pass one wave of
-// about one tile per SM, and the look-back reads 16 predecessors per L2 round
-// trip, so the prefix crosses a wave in a handful of round trips; staging
-// the tile before the look-back overlaps that wait with useful work.
+// about two tiles per SM, and the look-back reads 16 predecessors per L2
+// round trip, so the prefix crosses a wave in a handful of round trips;
+// staging the tile before the look-back overlaps that wait with useful work.
 // Ping-pong between the caller's buffers and scratch; after an even number
 // of passes the result is back in the caller's buffers (as in the reference),
 // after an odd number it is copied back.
@@ -29,8 +29,13 @@ namespace wfpt {
 
 cudaError_t status_sort(uint32_t* out) { return read_and_clear_status(out); }
 
-constexpr int kSortThreads = 1024;
+constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
+// Resident pass CTAs per SM (registers: 2 x 512 threads x 64; shared
+// memory: two large-tile CTAs fit in an SM's 228 KB).  Two CTAs let one
+// tile's ranking overlap the other's scatter and look-back wait; one
+// 1024-thread CTA per SM was 17-18 % slower on 2^24-2^26 keys.
+constexpr int kSortCtasPerSm = 2;
 constexpr int kRadix = 256;
 constexpr int kHistBlock = 256;
 constexpr uint32_t kLbAggregate = 1u << 30;
@@ -38,8 +43,11 @@ constexpr uint32_t kLbPrefix = 2u << 30;
 constexpr uint32_t kLbValue = (1u << 30) - 1u;
 constexpr int kLbChunk = 16;  // predecessors read per look-back round trip
 
-// Keys per thread of the two tile variants (tile = 1024 * KPT keys).
-constexpr int kKptSmall32 = 8, kKptLarge32 = 16;
+// Keys per thread of the tile variants (tile = 512 * KPT keys).  32-bit
+// keys have a third, extra-large variant for sorts of many waves (10 %
+// faster than 16 keys per thread on 2^26 keys); for 64-bit keys the large
+// tile is already the largest that leaves room for two CTAs per SM.
+constexpr int kKptSmall32 = 8, kKptLarge32 = 16, kKptXLarge32 = 20;
 constexpr int kKptSmall64 = 8, kKptLarge64 = 14;
 
 // Digit mask of pass p with db-bit digits: the top pass keeps only the
@@ -144,7 +152,7 @@ static void launch_hist(const K* keys, uint32_t n, const uint32_t* n_dev, int pa
 // count is the sum of the 16 byte bins sharing that nibble (nibble 0: low
 // nibble of the byte, 1: high nibble).
 template <typename K, int KPT, int DB>
-__global__ void __launch_bounds__(kSortThreads, 1) k_onesweep(const K* __restrict__ keys_in,
+__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const K* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               K* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n,
@@ -338,6 +346,8 @@ cudaError_t sort_prepare() {
     if (g_num_sms != 0) return cudaSuccess;
     cudaError_t e = opt_in_smem<uint32_t, kKptSmall32, 8>();
     if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptLarge32, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptXLarge32, 8>();
+    if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptXLarge32, 4>();
     if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptSmall64, 8>();
     if (e == cudaSuccess) e = opt_in_smem<uint64_t, kKptLarge64, 8>();
     if (e == cudaSuccess) e = opt_in_smem<uint32_t, kKptSmall32, 4>();
@@ -351,11 +361,12 @@ cudaError_t sort_prepare() {
     return e;
 }
 
-// Tile variant: 0 = automatic, 1 = small tiles, 2 = large tiles.  Automatic
-// takes the small tiles while they fit in one wave (one tile per SM) and the
-// large ones otherwise, which halves the waves of a frame-sized sort.
+// Tile variant: 0 = automatic, 1 = small, 2 = large, 3 = extra-large tiles
+// (64-bit keys: same as large).  Automatic takes the small tiles while they
+// fit in one wave (two tiles per SM), the large ones while those fit in two
+// waves (a frame-sized sort), and the extra-large ones beyond.
 static int g_sort_tiles = 0;
-void set_sort_tiles(int v) { g_sort_tiles = v < 0 ? 0 : (v > 2 ? 2 : v); }
+void set_sort_tiles(int v) { g_sort_tiles = v < 0 ? 0 : (v > 3 ? 3 : v); }
 int get_sort_tiles() { return g_sort_tiles; }
 
 // Digit width: 8 (default) or 4 bits per pass (twice the passes, 16-bin
@@ -364,10 +375,13 @@ static int g_digit_bits = 8;
 void set_sort_digit_bits(int v) { g_digit_bits = v == 4 ? 4 : 8; }
 int get_sort_digit_bits() { return g_digit_bits; }
 
-static bool use_large_tiles(uint32_t n, bool wide) {
-    if (g_sort_tiles != 0) return g_sort_tiles == 2;
+static int tile_variant(uint32_t n, bool wide) {
+    if (g_sort_tiles != 0) return g_sort_tiles;
+    const size_t slots = (size_t)g_num_sms * kSortCtasPerSm;
     const size_t small = (size_t)kSortThreads * (wide ? kKptSmall64 : kKptSmall32);
-    return ((size_t)n + small - 1) / small > (size_t)g_num_sms;
+    const size_t large = (size_t)kSortThreads * (wide ? kKptLarge64 : kKptLarge32);
+    if (((size_t)n + small - 1) / small <= slots) return 1;
+    return ((size_t)n + large - 1) / large <= 2 * slots ? 2 : 3;
 }
 
 struct SortLayout {
@@ -453,13 +467,17 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     constexpr bool wide = sizeof(K) == 8;
-    constexpr int large = wide ? kKptLarge64 : kKptLarge32, small = wide ? kKptSmall64 : kKptSmall32;
-    const bool lt = use_large_tiles(n, wide);
-    if (g_digit_bits == 4)
-        return lt ? sort_passes<K, large, 4>(keys, values, n, n_dev, key_bits, L, scratch, s)
-                  : sort_passes<K, small, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
-    return lt ? sort_passes<K, large, 8>(keys, values, n, n_dev, key_bits, L, scratch, s)
-              : sort_passes<K, small, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    constexpr int small = wide ? kKptSmall64 : kKptSmall32, large = wide ? kKptLarge64 : kKptLarge32;
+    constexpr int xlarge = wide ? kKptLarge64 : kKptXLarge32;
+    const int tv = tile_variant(n, wide);
+    if (g_digit_bits == 4) {
+        if (tv == 1) return sort_passes<K, small, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
+        if (tv == 2) return sort_passes<K, large, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
+        return sort_passes<K, xlarge, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    }
+    if (tv == 1) return sort_passes<K, small, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    if (tv == 2) return sort_passes<K, large, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
+    return sort_passes<K, xlarge, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
 }
 
 cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,

@@ -73,6 +73,10 @@ cudaError_t launch_morton(const wfpt_ray* rays, uint32_t n, const uint32_t* n_de
 cudaError_t launch_reorder(const uint32_t* idx, const wfpt_ray* in_rays, wfpt_ray* out_rays,
                            const int32_t* in_s2i, int32_t* out_s2i, int32_t* out_i2s, uint32_t n,
                            const uint32_t* n_dev, cudaStream_t s);
+// record_bytes 16, 32, 48 or 64; slot maps optional (all three or none).
+cudaError_t launch_reorder_records(const uint32_t* idx, const void* in_records, void* out_records,
+                                   uint32_t record_bytes, const int32_t* in_s2i, int32_t* out_s2i, int32_t* out_i2s,
+                                   uint32_t n, const uint32_t* n_dev, cudaStream_t s);
 
 // sort.cu
 size_t sort_scratch_bytes(uint32_t max_n, int key_bits);
