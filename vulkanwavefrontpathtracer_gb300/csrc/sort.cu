@@ -145,39 +145,21 @@ static void launch_hist(const K* keys, uint32_t n, const uint32_t* n_dev, int pa
     }
 }
 
-// One digit pass with DB-bit digits (RADIX = 2^DB bins).  Dynamic shared
-// memory: TILE keys, TILE values, kSortWarps*RADIX per-warp digit
-// counters, RADIX global bases, RADIX local offsets.  hist is the byte
-// histogram (k_sort_hist) of this pass's byte; with 4-bit digits a digit's
-// count is the sum of the 16 byte bins sharing that nibble (nibble 0: low
-// nibble of the byte, 1: high nibble).
-template <typename K, int KPT, int DB>
-__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const K* __restrict__ keys_in,
-                                                              const uint32_t* __restrict__ vals_in,
-                                                              K* __restrict__ keys_out,
-                                                              uint32_t* __restrict__ vals_out, uint32_t n,
-                                                              const uint32_t* __restrict__ n_dev, int shift,
-                                                              uint32_t dmask, const uint32_t* __restrict__ hist,
-                                                              uint32_t* __restrict__ lookback,
-                                                              uint32_t* __restrict__ ticket, int nibble) {
+// One tile of a digit pass (below).  FULL: the tile holds TILE keys, so
+// the per-key bounds checks of the last, partial tile drop out.
+template <typename K, int KPT, int DB, bool FULL>
+__device__ __forceinline__ void onesweep_tile(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                              K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                              uint32_t count, uint32_t tile, int shift, uint32_t dmask,
+                                              const uint32_t* __restrict__ hist, uint32_t* __restrict__ lookback,
+                                              int nibble, unsigned char* smem, uint32_t* s_scan) {
     constexpr uint32_t TILE = kSortThreads * KPT;
     constexpr int kRadix = 1 << DB;
-    extern __shared__ __align__(16) unsigned char smem[];
     K* s_keys = reinterpret_cast<K*>(smem);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
     uint32_t* s_hist = s_vals + TILE;  // [warp][digit]
     uint32_t* s_base = s_hist + kSortWarps * kRadix;
     uint32_t* s_loc = s_base + kRadix;
-    __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_scan[kSortWarps];
-
-    const uint32_t count = load_count(n, n_dev);
-    const uint32_t ntiles = (count + TILE - 1) / TILE;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    if (tile >= ntiles) return;
 
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -188,20 +170,20 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         uint32_t i = base + k * 32;
-        key[k] = i < count ? keys_in[i] : (K)0;
+        key[k] = (FULL || i < count) ? keys_in[i] : (K)0;
     }
     uint32_t* my_hist = s_hist + warp * kRadix;
     // Warp-level stable ranking: keys are visited in input order (k, lane).
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
-        bool ok = (base + k * 32) < count;
+        const bool ok = FULL || (base + k * 32) < count;
         uint32_t d = digit_of(key[k], shift, dmask);
-        uint32_t peers = __ballot_sync(0xffffffffu, ok);
+        uint32_t peers = FULL ? 0xffffffffu : __ballot_sync(0xffffffffu, ok);
 #pragma unroll
         for (int b = 0; b < DB; ++b) {
             uint32_t bit = (d >> b) & 1u;
             uint32_t m = __ballot_sync(0xffffffffu, bit);
-            peers &= bit ? m : ~m;
+            peers &= m ^ (bit - 1u);  // m where the bit is set, ~m where clear
         }
         uint32_t before = peers & lt_mask;
         uint32_t pre = ok ? my_hist[d] : 0u;
@@ -254,7 +236,7 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         uint32_t i = base + k * 32;
-        if (i < count) {
+        if (FULL || i < count) {
             uint32_t dk = digit_of(key[k], shift, dmask);
             uint32_t pos = s_loc[dk] + my_hist[dk] + rank[k];
             s_keys[pos] = key[k];
@@ -299,7 +281,8 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
     if (owner) s_base[d] = excl - loc;
     __syncthreads();
 
-    const uint32_t tile_count = min(TILE, count - tile * TILE);
+    const uint32_t tile_count = FULL ? TILE : min(TILE, count - tile * TILE);
+#pragma unroll 2
     for (uint32_t j = threadIdx.x; j < tile_count; j += kSortThreads) {
         K kk = s_keys[j];
         uint32_t g = s_base[digit_of(kk, shift, dmask)] + j;
@@ -310,6 +293,43 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
             raise_status(kErrBounds);
         }
     }
+}
+
+// One digit pass with DB-bit digits (RADIX = 2^DB bins).  Dynamic shared
+// memory: TILE keys, TILE values, kSortWarps*RADIX per-warp digit
+// counters, RADIX global bases, RADIX local offsets.  hist is the byte
+// histogram (k_sort_hist) of this pass's byte; with 4-bit digits a digit's
+// count is the sum of the 16 byte bins sharing that nibble (nibble 0: low
+// nibble of the byte, 1: high nibble).
+template <typename K, int KPT, int DB>
+__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const K* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              K* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, uint32_t n,
+                                                              const uint32_t* __restrict__ n_dev, int shift,
+                                                              uint32_t dmask, const uint32_t* __restrict__ hist,
+                                                              uint32_t* __restrict__ lookback,
+                                                              uint32_t* __restrict__ ticket, int nibble) {
+    constexpr uint32_t TILE = kSortThreads * KPT;
+    constexpr int kRadix = 1 << DB;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* s_hist = reinterpret_cast<uint32_t*>(smem + (size_t)TILE * (sizeof(K) + 4));
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_scan[kSortWarps];
+
+    const uint32_t count = load_count(n, n_dev);
+    const uint32_t ntiles = (count + TILE - 1) / TILE;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) return;
+    if ((size_t)(tile + 1) * TILE <= count)
+        onesweep_tile<K, KPT, DB, true>(keys_in, vals_in, keys_out, vals_out, count, tile, shift, dmask, hist,
+                                        lookback, nibble, smem, s_scan);
+    else
+        onesweep_tile<K, KPT, DB, false>(keys_in, vals_in, keys_out, vals_out, count, tile, shift, dmask, hist,
+                                         lookback, nibble, smem, s_scan);
 }
 
 // After an odd number of passes: move the first `count` pairs back into the
