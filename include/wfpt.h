@@ -133,6 +133,10 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          3 = extra-large tiles (32-bit keys; 64-bit keys
  *                          take the large ones)
  *   "sort.digit_bits"      radix digit width per pass: 8 (default) or 4
+ *   "build.bvh8.collapse"  BVH8 collapse of scenes built afterwards: 1 = SAH
+ *                          dynamic programme (default), 0 = greedy fill
+ *   "build.bvh8.tri_cost"  triangle-test cost relative to a node step in the
+ *                          SAH collapse, percent (1..10000, default 20)
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */

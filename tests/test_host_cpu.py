@@ -155,9 +155,19 @@ def test_tiny_and_empty_scenes_build(wf, ntris):
     sc.close()
 
 
-def test_bvh8_boxes_are_conservative(wf):
+@pytest.mark.parametrize("collapse,tri_cost", [(1, 20), (1, 100), (0, 100)])
+def test_bvh8_boxes_are_conservative(wf, collapse, tri_cost):
+    """Every child box holds its subtree's triangles, every triangle appears
+    once, for the SAH collapse (two cost ratios) and the greedy one."""
     pos, _, idx = wf.api.generate_scene(0, 4, 4000)
-    sc = wf.api.Scene(pos, idx, host_only=True)
+    old = wf.api.tune_get("build.bvh8.collapse"), wf.api.tune_get("build.bvh8.tri_cost")
+    try:
+        wf.api.tune_set("build.bvh8.collapse", collapse)
+        wf.api.tune_set("build.bvh8.tri_cost", tri_cost)
+        sc = wf.api.Scene(pos, idx, host_only=True)
+    finally:
+        wf.api.tune_set("build.bvh8.collapse", old[0])
+        wf.api.tune_set("build.bvh8.tri_cost", old[1])
     nodes_u8, tris_u8 = sc.export_bvh8()
     nb = nodes_u8.reshape(-1, 80)
     tris = tris_u8.view(np.float32).reshape(-1, 12)
@@ -289,7 +299,8 @@ def test_tuning_knobs(wf):
         assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
         assert api.tune_get("trace.bvh8.coop") == 0
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
-                         ("trace.bvh8.coop", 2), ("sort.tiles", 4), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("no.such.knob", 1)):
+                         ("trace.bvh8.coop", 2), ("sort.tiles", 4), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("build.bvh8.collapse", 2),
+                         ("build.bvh8.tri_cost", 0), ("build.bvh8.tri_cost", 10001), ("no.such.knob", 1)):
             with pytest.raises(wf.WfptError):
                 api.tune_set(key, bad)
     finally:

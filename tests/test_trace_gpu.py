@@ -75,6 +75,33 @@ def test_bvh8_equals_bvh2(wf, dev, scene, request):
     assert wf.api.device_status() == 0
 
 
+@pytest.mark.parametrize("collapse,tri_cost", [(0, 100), (1, 100), (1, 5)])
+def test_bvh8_collapse_policies_equal_bvh2(wf, dev, collapse, tri_cost):
+    """The greedy and SAH collapses (different tree shapes and leaf sizes)
+    give the BVH2's closest hits on the courtyard."""
+    pos, nrm, idx = wf.api.generate_scene(1, 1)
+    old = wf.api.tune_get("build.bvh8.collapse"), wf.api.tune_get("build.bvh8.tri_cost")
+    try:
+        wf.api.tune_set("build.bvh8.collapse", collapse)
+        wf.api.tune_set("build.bvh8.tri_cost", tri_cost)
+        sc = wf.api.Scene(pos, idx)
+    finally:
+        wf.api.tune_set("build.bvh8.collapse", old[0])
+        wf.api.tune_set("build.bvh8.tri_cost", old[1])
+    lo, hi = sc.bounds_min, sc.bounds_max
+    rng = np.random.default_rng(13)
+    n = 200000
+    rays = random_rays(rng, n, tmax=1e30)
+    rays[:, :3] = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    g2 = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
+    g8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays)
+    assert np.array_equal(g2, g8)
+    a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)
+    assert np.array_equal(a8[:, 0] >= 0, g2[:, 0] >= 0)
+    sc.close()
+    assert wf.api.device_status() == 0
+
+
 @pytest.mark.parametrize("kind", [0, 1])
 def test_against_fp64(wf, orc, dev, soup, kind):
     pos, idx, sc = soup

@@ -112,6 +112,16 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_sort_digit_bits((int)value);
         return WFPT_OK;
     }
+    if (k == "build.bvh8.collapse") {
+        if (value < 0 || value > 1) return invalid("build.bvh8.collapse must be 0 (greedy) or 1 (SAH)");
+        wfpt::set_bvh8_collapse((int)value);
+        return WFPT_OK;
+    }
+    if (k == "build.bvh8.tri_cost") {
+        if (value < 1 || value > 10000) return invalid("build.bvh8.tri_cost must be in [1, 10000] percent");
+        wfpt::set_bvh8_tri_cost_pct((int)value);
+        return WFPT_OK;
+    }
     if (k == "trace.count") {
         if (value < 0 || value > 1) return invalid("trace.count must be 0 or 1");
         wfpt::set_trace_count(value != 0);
@@ -148,6 +158,14 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "sort.digit_bits") {
         *value = wfpt::get_sort_digit_bits();
+        return WFPT_OK;
+    }
+    if (k == "build.bvh8.collapse") {
+        *value = wfpt::get_bvh8_collapse();
+        return WFPT_OK;
+    }
+    if (k == "build.bvh8.tri_cost") {
+        *value = wfpt::get_bvh8_tri_cost_pct();
         return WFPT_OK;
     }
     if (k == "trace.count") {

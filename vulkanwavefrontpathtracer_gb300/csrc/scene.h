@@ -73,8 +73,15 @@ struct BuildInput {
 
 // Binned-SAH BVH2 build with leaves of at most max_leaf triangles.
 void build_bvh2(const BuildInput& in, int max_leaf, HostBvh2& out);
-// Greedy collapse of a BVH2 (leaves <= 3 triangles) into the 8-wide format.
+// Collapse of a BVH2 into the 8-wide format (leaf children <= 3 triangles),
+// by the policy below.
 void build_bvh8(const HostBvh2& bvh2, HostBvh8& out);
+// Collapse policy: 1 = SAH dynamic programme (default), 0 = greedy; the
+// triangle-test cost relative to a node step in percent (default 20).
+void set_bvh8_collapse(int mode);
+int get_bvh8_collapse();
+void set_bvh8_tri_cost_pct(int pct);
+int get_bvh8_tri_cost_pct();
 
 // Persistent-traversal work counters: kWorkSlots slots of 16 u32 each
 // (next ray, warps finished), zeroed at scene creation.
