@@ -357,11 +357,31 @@ typedef struct wfpt_scene_info {
  * WFPT_SCENE_HOST_ONLY to build on the host without uploading (such a scene
  * can be exported but not traced). */
 #define WFPT_SCENE_HOST_ONLY 0x100
+/* bvh_kinds_mask flag: upload the mesh and build both BVHs on the device
+ * (wfpt_scene_create_device) instead of on the host.  Scenes of fewer than
+ * two triangles are built on the host either way. */
+#define WFPT_SCENE_DEVICE_BUILD 0x200
 wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices,
                               const uint32_t* indices, uint32_t num_triangles,
                               const uint32_t* geometry_first_triangle,
                               uint32_t num_geometries, int bvh_kinds_mask,
                               wfpt_scene** scene);
+/* Device build from geometry already in device memory: positions_dev
+ * float[3*num_vertices], indices_dev uint32[3*num_triangles];
+ * geometry_first_triangle stays a host array.  No reference counterpart
+ * beyond the AS build it replaces (WaveFrontPathTracer.cpp:202-457, driver
+ * BLAS build with PREFER_FAST_TRACE): the BVH2 by PLOC clustering of
+ * Morton-sorted triangle centroids, the BVH8 by the same SAH collapse as the
+ * host build (knobs "build.bvh8.*").  Hits equal those of a host-built scene
+ * of the same mesh (the traversal result does not depend on the tree).
+ * Runs on `stream` and returns when the scene is ready; out-of-range
+ * triangle indices return WFPT_ERR_INVALID_ARGUMENT.  Exports of such a
+ * scene copy its device buffers. */
+wfpt_status wfpt_scene_create_device(const float* positions_dev, uint32_t num_vertices,
+                                     const uint32_t* indices_dev, uint32_t num_triangles,
+                                     const uint32_t* geometry_first_triangle,
+                                     uint32_t num_geometries, int bvh_kinds_mask,
+                                     void* stream, wfpt_scene** scene);
 void wfpt_scene_destroy(wfpt_scene* scene);
 wfpt_status wfpt_scene_get_info(const wfpt_scene* scene, wfpt_scene_info* info);
 /* Host copies of the BVH2 (FP32 nodes, 64 B each) and its triangle table

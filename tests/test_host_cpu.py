@@ -53,6 +53,11 @@ def test_invalid_arguments_rejected_on_host(wf):
     assert b"aligned" in lib.wfpt_last_error_message()
     assert lib.wfpt_reorder_records(buf, buf, buf, 48, None, None, None, 4, None, None) == 1  # in place
     assert lib.wfpt_reorder_records(None, None, None, 48, None, None, None, 0, None, None) == 0  # empty
+    out = C.c_void_p()
+    assert lib.wfpt_scene_create_device(None, 3, None, 5, None, 0, 3, None, C.byref(out)) == 1  # null mesh
+    assert lib.wfpt_scene_create_device(buf, 3, buf, 5, None, 0, 3 | 0x100, None, C.byref(out)) == 1  # host-only
+    assert lib.wfpt_scene_create_device(buf, 0, buf, 5, None, 0, 3, None, C.byref(out)) == 1  # no vertices
+    assert lib.wfpt_scene_create_device(buf, 3, buf, 5, None, 0, 0, None, C.byref(out)) == 1  # no BVH kind
     assert lib.wfpt_raygen_shadow(buf, buf, buf, buf, buf, buf, wf._lib.fvec([0, 0, 0]), 1.0, 0, 4, None, 0,
                                   None) == 1
     assert lib.wfpt_trace(None, 0, buf, buf, None, 4, None, 1, None) == 1

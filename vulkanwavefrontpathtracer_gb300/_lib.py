@@ -155,6 +155,8 @@ _SIGS = {
     "wfpt_interpolate_colors": (c_int, [c_void_p, c_void_p, c_u32, c_int, c_float, c_float, c_void_p]),
     "wfpt_fill_u32": (c_int, [c_void_p, c_u32, c_size_t, c_void_p]),
     "wfpt_scene_create": (c_int, [c_void_p, c_u32, c_void_p, c_u32, c_void_p, c_u32, c_int, C.POINTER(c_void_p)]),
+    "wfpt_scene_create_device": (c_int, [c_void_p, c_u32, c_void_p, c_u32, c_void_p, c_u32, c_int, c_void_p,
+                                         C.POINTER(c_void_p)]),
     "wfpt_scene_destroy": (None, [c_void_p]),
     "wfpt_scene_get_info": (c_int, [c_void_p, C.POINTER(SceneInfo)]),
     "wfpt_scene_export_bvh2": (c_int, [c_void_p, c_void_p, P_size, c_void_p, P_size]),

@@ -266,16 +266,41 @@ class Scene:
     """Acceleration structures of one triangle mesh (replaces the BLAS/TLAS)."""
 
     HOST_ONLY = 0x100
+    DEVICE_BUILD = 0x200
 
-    def __init__(self, positions, indices, geometry_first=None, bvh2=True, bvh8=True, host_only=False):
-        positions = np.ascontiguousarray(positions, np.float32)
-        indices = np.ascontiguousarray(indices, np.uint32)
+    def __init__(self, positions, indices, geometry_first=None, bvh2=True, bvh8=True, host_only=False,
+                 device_build=False, _handle=None):
+        if _handle is not None:
+            h = _handle
+        else:
+            positions = np.ascontiguousarray(positions, np.float32)
+            indices = np.ascontiguousarray(indices, np.uint32)
+            gf = None if geometry_first is None else np.ascontiguousarray(geometry_first, np.uint32)
+            mask = ((1 if bvh2 else 0) | (2 if bvh8 else 0) | (self.HOST_ONLY if host_only else 0)
+                    | (self.DEVICE_BUILD if device_build else 0))
+            h = C.c_void_p()
+            L.check(lib().wfpt_scene_create(positions.ctypes.data, positions.shape[0], indices.ctypes.data,
+                                            indices.shape[0], None if gf is None else gf.ctypes.data,
+                                            0 if gf is None else gf.shape[0], mask, C.byref(h)))
+        self._init_from_handle(h)
+
+    @classmethod
+    def from_device(cls, positions, indices, geometry_first=None, bvh2=True, bvh8=True, stream=None):
+        """Builds the BVHs on the GPU from device tensors: positions float32
+        (V, 3), indices int32/uint32 (T, 3); geometry_first a host array."""
+        if not (positions.is_cuda and indices.is_cuda):
+            raise ValueError("positions and indices must be device tensors")
+        positions = positions.contiguous()
+        indices = indices.contiguous()
         gf = None if geometry_first is None else np.ascontiguousarray(geometry_first, np.uint32)
-        mask = (1 if bvh2 else 0) | (2 if bvh8 else 0) | (self.HOST_ONLY if host_only else 0)
+        mask = (1 if bvh2 else 0) | (2 if bvh8 else 0)
         h = C.c_void_p()
-        L.check(lib().wfpt_scene_create(positions.ctypes.data, positions.shape[0], indices.ctypes.data,
-                                        indices.shape[0], None if gf is None else gf.ctypes.data,
-                                        0 if gf is None else gf.shape[0], mask, C.byref(h)))
+        L.check(lib().wfpt_scene_create_device(_p(positions), positions.shape[0], _p(indices), indices.shape[0],
+                                               None if gf is None else gf.ctypes.data,
+                                               0 if gf is None else gf.shape[0], mask, _s(stream), C.byref(h)))
+        return cls(None, None, _handle=h)
+
+    def _init_from_handle(self, h):
         self.handle = h
         info = L.SceneInfo()
         L.check(lib().wfpt_scene_get_info(h, C.byref(info)))

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/wfpt.h"
+#include "build.cuh"
 #include "host.h"
 #include "internal.h"
 #include "scene.h"
@@ -46,6 +47,8 @@ struct wfpt_scene {
     void* bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     wfpt_scene_info info{};
     bool has2 = false, has8 = false, host_only = false;
+    bool device_built = false;  // BVHs built on the GPU: no host copies
+    uint32_t dev_bvh2_count = 0, dev_bvh8_count = 0, dev_ntris = 0;
 };
 
 namespace wfpt {
@@ -182,6 +185,7 @@ wfpt_status wfpt_device_status(uint32_t* flags) {
     if ((e = wfpt::status_stages(&v)) != cudaSuccess) return from_cuda(e);
     if ((e = wfpt::status_sort(&v)) != cudaSuccess) return from_cuda(e);
     if ((e = wfpt::status_trace(&v)) != cudaSuccess) return from_cuda(e);
+    if ((e = wfpt::status_build(&v)) != cudaSuccess) return from_cuda(e);
     if (flags) *flags = v;
     if (v & wfpt::kStatusTimeout) {
         g_last_error = "a bounded device-side wait gave up";
@@ -401,6 +405,120 @@ static cudaError_t upload(void** dst, const void* src, size_t bytes) {
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
 }
 
+static wfpt_status check_geometry_table(const uint32_t* geometry_first_triangle, uint32_t num_geometries,
+                                        uint32_t num_triangles) {
+    if (geometry_first_triangle && num_geometries > 0) {
+        WFPT_REQUIRE(geometry_first_triangle[0] == 0, "geometry_first_triangle[0] must be 0");
+        for (uint32_t g = 1; g < num_geometries; ++g)
+            WFPT_REQUIRE(geometry_first_triangle[g] >= geometry_first_triangle[g - 1] &&
+                             geometry_first_triangle[g] <= num_triangles,
+                         "geometry_first_triangle must ascend within [0, num_triangles]");
+    }
+    return WFPT_OK;
+}
+
+// A scene whose BVHs are built on the device from device-resident geometry
+// (at least two triangles; build.cu).
+static wfpt_status create_device_built(const float* positions_dev, uint32_t num_vertices,
+                                       const uint32_t* indices_dev, uint32_t num_triangles,
+                                       const uint32_t* geometry_first_triangle, uint32_t num_geometries,
+                                       int bvh_kinds_mask, cudaStream_t s,
+                                       std::chrono::steady_clock::time_point t0, wfpt_scene** scene) {
+    std::vector<uint32_t> gf(num_geometries ? num_geometries : 1u, 0u);
+    if (geometry_first_triangle && num_geometries)
+        std::memcpy(gf.data(), geometry_first_triangle, gf.size() * sizeof(uint32_t));
+    void* gdev = nullptr;
+    cudaError_t e = upload(&gdev, gf.data(), gf.size() * sizeof(uint32_t));
+    if (e != cudaSuccess) return from_cuda(e);
+    wfpt::DeviceBuild b;
+    e = wfpt::build_scene_device(positions_dev, num_vertices, indices_dev, num_triangles,
+                                 reinterpret_cast<const uint32_t*>(gdev), (uint32_t)gf.size(),
+                                 (bvh_kinds_mask & (1 << WFPT_BVH8_Q8)) != 0, s, &b);
+    cudaFree(gdev);
+    if (e == cudaErrorInvalidValue) return invalid("triangle index out of range");
+    if (e != cudaSuccess) {
+        wfpt_status st = from_cuda(e);
+        g_last_error = std::string("device BVH build failed: ") + g_last_error;
+        return st;
+    }
+    wfpt_scene* sc = new (std::nothrow) wfpt_scene();
+    if (!sc) {
+        for (void* p : {b.bvh2_nodes, b.bvh2_tris, b.bvh8_nodes, b.bvh8_tris, b.rec_of_key})
+            if (p) cudaFree(p);
+        return WFPT_ERR_OUT_OF_MEMORY;
+    }
+    sc->device_built = true;
+    sc->has2 = (bvh_kinds_mask & (1 << WFPT_BVH2_FP32)) != 0;
+    sc->has8 = (bvh_kinds_mask & (1 << WFPT_BVH8_Q8)) != 0;
+    if (sc->has2) {
+        sc->bufs[0] = b.bvh2_nodes;
+        sc->bufs[1] = b.bvh2_tris;
+    } else {
+        cudaFree(b.bvh2_nodes);
+        cudaFree(b.bvh2_tris);
+    }
+    sc->bufs[2] = b.bvh8_nodes;
+    sc->bufs[3] = b.bvh8_tris;
+    sc->bufs[5] = b.rec_of_key;
+    e = cudaMalloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(sc->bufs[4], 0, wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        wfpt_scene_destroy(sc);
+        return from_cuda(e);
+    }
+    sc->dev.work = reinterpret_cast<uint32_t*>(sc->bufs[4]);
+    sc->dev.bvh2_nodes = reinterpret_cast<const float4*>(sc->bufs[0]);
+    sc->dev.bvh2_tris = reinterpret_cast<const float4*>(sc->bufs[1]);
+    sc->dev.bvh8_nodes = reinterpret_cast<const float4*>(sc->bufs[2]);
+    sc->dev.bvh8_tris = reinterpret_cast<const float4*>(sc->bufs[3]);
+    sc->dev.bvh8_rec_of_key = reinterpret_cast<const uint32_t*>(sc->bufs[5]);
+    sc->dev.bvh8_num_tris = sc->has8 ? num_triangles : 0u;
+    sc->dev_bvh2_count = sc->has2 ? b.bvh2_count : 0u;
+    sc->dev_bvh8_count = sc->has8 ? b.bvh8_count : 0u;
+    sc->dev_ntris = num_triangles;
+    sc->info.num_triangles = num_triangles;
+    sc->info.num_geometries = (uint32_t)gf.size();
+    sc->info.bvh2_nodes = sc->dev_bvh2_count;
+    sc->info.bvh8_nodes = sc->dev_bvh8_count;
+    for (int k = 0; k < 3; ++k) {
+        sc->info.bounds_min[k] = b.bounds_min[k];
+        sc->info.bounds_max[k] = b.bounds_max[k];
+    }
+    sc->info.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *scene = sc;
+    return WFPT_OK;
+}
+
+wfpt_status wfpt_scene_create_device(const float* positions_dev, uint32_t num_vertices,
+                                     const uint32_t* indices_dev, uint32_t num_triangles,
+                                     const uint32_t* geometry_first_triangle, uint32_t num_geometries,
+                                     int bvh_kinds_mask, void* stream, wfpt_scene** scene) {
+    WFPT_REQUIRE(scene, "null scene out-pointer");
+    *scene = nullptr;
+    WFPT_REQUIRE(num_triangles == 0 || (positions_dev && indices_dev), "null mesh");
+    WFPT_REQUIRE(num_triangles < (1u << 27), "too many triangles (max 2^27 - 1)");
+    WFPT_REQUIRE((bvh_kinds_mask & 3) != 0, "bvh_kinds_mask selects no BVH");
+    WFPT_REQUIRE((bvh_kinds_mask & WFPT_SCENE_HOST_ONLY) == 0, "a device-built scene cannot be host-only");
+    WFPT_REQUIRE(num_triangles == 0 || num_vertices > 0, "triangles without vertices");
+    wfpt_status st = check_geometry_table(geometry_first_triangle, num_geometries, num_triangles);
+    if (st != WFPT_OK) return st;
+    auto t0 = std::chrono::steady_clock::now();
+    if (num_triangles < 2) {
+        // One triangle or none: the host builder's wrapped or empty root.
+        std::vector<uint32_t> idx(3ull * num_triangles);
+        std::vector<float> pos(3ull * num_vertices);
+        cudaError_t e = cudaSuccess;
+        if (!idx.empty()) e = cudaMemcpy(idx.data(), indices_dev, idx.size() * 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && !pos.empty())
+            e = cudaMemcpy(pos.data(), positions_dev, pos.size() * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return from_cuda(e);
+        return wfpt_scene_create(pos.data(), num_vertices, idx.data(), num_triangles, geometry_first_triangle,
+                                 num_geometries, bvh_kinds_mask & 3, scene);
+    }
+    return create_device_built(positions_dev, num_vertices, indices_dev, num_triangles, geometry_first_triangle,
+                               num_geometries, bvh_kinds_mask & 3, S(stream), t0, scene);
+}
+
 wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, const uint32_t* indices,
                               uint32_t num_triangles, const uint32_t* geometry_first_triangle,
                               uint32_t num_geometries, int bvh_kinds_mask, wfpt_scene** scene) {
@@ -409,16 +527,27 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
     WFPT_REQUIRE(num_triangles == 0 || (positions && indices), "null mesh");
     WFPT_REQUIRE(num_triangles < (1u << 27), "too many triangles (max 2^27 - 1)");
     WFPT_REQUIRE((bvh_kinds_mask & 3) != 0, "bvh_kinds_mask selects no BVH");
+    WFPT_REQUIRE((bvh_kinds_mask & WFPT_SCENE_HOST_ONLY) == 0 || (bvh_kinds_mask & WFPT_SCENE_DEVICE_BUILD) == 0,
+                 "a device-built scene cannot be host-only");
     for (uint64_t i = 0; i < 3ull * num_triangles; ++i)
         if (indices[i] >= num_vertices) return invalid("triangle index out of range");
-    if (geometry_first_triangle && num_geometries > 0) {
-        WFPT_REQUIRE(geometry_first_triangle[0] == 0, "geometry_first_triangle[0] must be 0");
-        for (uint32_t g = 1; g < num_geometries; ++g)
-            WFPT_REQUIRE(geometry_first_triangle[g] >= geometry_first_triangle[g - 1] &&
-                             geometry_first_triangle[g] <= num_triangles,
-                         "geometry_first_triangle must ascend within [0, num_triangles]");
-    }
+    wfpt_status gst = check_geometry_table(geometry_first_triangle, num_geometries, num_triangles);
+    if (gst != WFPT_OK) return gst;
     auto t0 = std::chrono::steady_clock::now();
+    if ((bvh_kinds_mask & WFPT_SCENE_DEVICE_BUILD) && num_triangles >= 2) {
+        void* pd = nullptr;
+        void* id = nullptr;
+        cudaError_t e = upload(&pd, positions, 3ull * num_vertices * sizeof(float));
+        if (e == cudaSuccess) e = upload(&id, indices, 3ull * num_triangles * sizeof(uint32_t));
+        wfpt_status st = e == cudaSuccess ? WFPT_OK : from_cuda(e);
+        if (st == WFPT_OK)
+            st = create_device_built(reinterpret_cast<const float*>(pd), num_vertices,
+                                     reinterpret_cast<const uint32_t*>(id), num_triangles, geometry_first_triangle,
+                                     num_geometries, bvh_kinds_mask & 3, nullptr, t0, scene);
+        if (pd) cudaFree(pd);
+        if (id) cudaFree(id);
+        return st;
+    }
     wfpt_scene* sc = new (std::nothrow) wfpt_scene();
     if (!sc) return WFPT_ERR_OUT_OF_MEMORY;
     wfpt::BuildInput in{positions, num_vertices, indices, num_triangles, geometry_first_triangle,
@@ -518,9 +647,31 @@ wfpt_status wfpt_scene_get_info(const wfpt_scene* scene, wfpt_scene_info* info) 
     return WFPT_OK;
 }
 
+// Exports of a device-built scene: copies of its device buffers.
+static wfpt_status export_device(const void* dnodes, size_t nb, const void* dtris, size_t tb, void* nodes,
+                                 size_t* node_bytes, void* triangles, size_t* triangle_bytes) {
+    cudaError_t e = cudaSuccess;
+    if (nodes) {
+        WFPT_REQUIRE(*node_bytes >= nb, "node buffer too small");
+        if (nb) e = cudaMemcpy(nodes, dnodes, nb, cudaMemcpyDeviceToHost);
+    }
+    if (triangles && e == cudaSuccess) {
+        WFPT_REQUIRE(*triangle_bytes >= tb, "triangle buffer too small");
+        if (tb) e = cudaMemcpy(triangles, dtris, tb, cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) return from_cuda(e);
+    *node_bytes = nb;
+    *triangle_bytes = tb;
+    return WFPT_OK;
+}
+
 wfpt_status wfpt_scene_export_bvh2(const wfpt_scene* scene, void* nodes, size_t* node_bytes, void* triangles,
                                    size_t* triangle_bytes) {
     WFPT_REQUIRE(scene && node_bytes && triangle_bytes, "null pointer");
+    if (scene->device_built)
+        return export_device(scene->bufs[0], scene->dev_bvh2_count * sizeof(wfpt::Bvh2Node), scene->bufs[1],
+                             scene->has2 ? scene->dev_ntris * sizeof(wfpt::TriRec) : 0, nodes, node_bytes,
+                             triangles, triangle_bytes);
     size_t nb = scene->bvh2.nodes.size() * sizeof(wfpt::Bvh2Node);
     size_t tb = scene->bvh2.tris.size() * sizeof(wfpt::TriRec);
     if (nodes) {
@@ -539,6 +690,10 @@ wfpt_status wfpt_scene_export_bvh2(const wfpt_scene* scene, void* nodes, size_t*
 wfpt_status wfpt_scene_export_bvh8(const wfpt_scene* scene, void* nodes, size_t* node_bytes, void* triangles,
                                    size_t* triangle_bytes) {
     WFPT_REQUIRE(scene && node_bytes && triangle_bytes, "null pointer");
+    if (scene->device_built)
+        return export_device(scene->bufs[2], scene->dev_bvh8_count * sizeof(wfpt::Bvh8Node), scene->bufs[3],
+                             scene->has8 ? scene->dev_ntris * sizeof(wfpt::TriRec) : 0, nodes, node_bytes,
+                             triangles, triangle_bytes);
     size_t nb = scene->bvh8.nodes.size() * sizeof(wfpt::Bvh8Node);
     size_t tb = scene->bvh8.tris.size() * sizeof(wfpt::TriRec);
     if (nodes) {
