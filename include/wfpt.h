@@ -135,6 +135,8 @@ uint64_t wfpt_kernel_launch_count(void);
  *   "sort.digit_bits"      radix digit width per pass: 8 (default) or 4
  *   "build.bvh8.collapse"  BVH8 collapse of scenes built afterwards: 1 = SAH
  *                          dynamic programme (default), 0 = greedy fill
+ *   "build.ploc.radius"    device build: clusters on either side searched
+ *                          for a nearest neighbour (1..64, default 8)
  *   "build.bvh8.tri_cost"  triangle-test cost relative to a node step in the
  *                          SAH collapse, percent (1..10000, default 20)
  *   "trace.count"         1 = launch the counting traversal kernels, which

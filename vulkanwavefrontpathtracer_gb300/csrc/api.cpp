@@ -115,6 +115,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_sort_digit_bits((int)value);
         return WFPT_OK;
     }
+    if (k == "build.ploc.radius") {
+        if (value < 1 || value > 64) return invalid("build.ploc.radius must be in [1, 64]");
+        wfpt::set_ploc_radius((int)value);
+        return WFPT_OK;
+    }
     if (k == "build.bvh8.collapse") {
         if (value < 0 || value > 1) return invalid("build.bvh8.collapse must be 0 (greedy) or 1 (SAH)");
         wfpt::set_bvh8_collapse((int)value);
@@ -161,6 +166,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "sort.digit_bits") {
         *value = wfpt::get_sort_digit_bits();
+        return WFPT_OK;
+    }
+    if (k == "build.ploc.radius") {
+        *value = wfpt::get_ploc_radius();
         return WFPT_OK;
     }
     if (k == "build.bvh8.collapse") {

@@ -7,8 +7,8 @@
 //      library's radix sort;
 //   3. PLOC (Meister and Bittner, "Parallel Locally-Ordered Clustering for
 //      Bounding Volume Hierarchy Construction", IEEE TVCG 2018): every
-//      cluster picks the neighbour among the 16 on either side (in Morton
-//      order) whose merged box has the least surface area, mutual pairs
+//      cluster picks the neighbour among the 8 (knob) on either side (in
+//      Morton order) whose merged box has the least surface area, mutual pairs
 //      merge, the cluster list is compacted by a prefix sum, until one
 //      cluster is left;
 //   4. the BVH2 in the traversal format (children's boxes grown by 2^-22 P
@@ -33,10 +33,18 @@ namespace wfpt {
 
 cudaError_t status_build(uint32_t* out) { return read_and_clear_status(out); }
 
+// PLOC search radius (clusters on either side in Morton order).  On the
+// courtyard's bounce-1 rays 8 gave the fastest traversal of radii 8-64 (the
+// BVH8 from radius 8 traced closest hits 8 % faster than from 16, 13 %
+// faster than from 64).
+static int g_ploc_radius = 8;
+void set_ploc_radius(int r) { g_ploc_radius = r < 1 ? 1 : (r > 64 ? 64 : r); }
+int get_ploc_radius() { return g_ploc_radius; }
+
 namespace {
 
 constexpr int kBB = 256;      // threads per build block
-constexpr int kPlocR = 16;    // PLOC search radius
+constexpr int kPlocRMax = 64;  // largest PLOC search radius (knob build.ploc.radius)
 constexpr int kScanItems = 8;  // elements per thread of the prefix sum
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
@@ -279,18 +287,19 @@ cudaError_t exclusive_scan(const uint64_t* in, uint64_t* out, uint32_t n, const 
 }
 
 // ---------------------------------------------------------------- stage 3
-// Nearest neighbour of every cluster within kPlocR positions: the least
+// Nearest neighbour of every cluster within `radius` positions: the least
 // merged surface area, ties to the smaller position.  For a fixed cluster
 // that order is the order of (area, smaller position, larger position) over
 // pairs, so the pair that is least in that order over all pairs is mutual
 // and every iteration merges at least one pair.
 __global__ void __launch_bounds__(kBB) k_ploc_nn(const uint32_t* __restrict__ cl, uint32_t m,
                                                  const float4* __restrict__ nlo, const float4* __restrict__ nhi,
-                                                 uint32_t* __restrict__ nn) {
-    __shared__ float4 s_lo[kBB + 2 * kPlocR], s_hi[kBB + 2 * kPlocR];
+                                                 uint32_t* __restrict__ nn, int radius) {
+    __shared__ float4 s_lo[kBB + 2 * kPlocRMax], s_hi[kBB + 2 * kPlocRMax];
+    const int R = radius < 1 ? 1 : (radius > kPlocRMax ? kPlocRMax : radius);
     const int b0 = (int)(blockIdx.x * kBB);
-    for (int t = threadIdx.x; t < kBB + 2 * kPlocR; t += kBB) {
-        const int j = b0 - kPlocR + t;
+    for (int t = threadIdx.x; t < kBB + 2 * R; t += kBB) {
+        const int j = b0 - R + t;
         if (j >= 0 && j < (int)m) {
             const uint32_t id = cl[j];
             s_lo[t] = nlo[id];
@@ -300,12 +309,12 @@ __global__ void __launch_bounds__(kBB) k_ploc_nn(const uint32_t* __restrict__ cl
     __syncthreads();
     const int i = b0 + (int)threadIdx.x;
     if (i >= (int)m) return;
-    const float4 alo = s_lo[threadIdx.x + kPlocR], ahi = s_hi[threadIdx.x + kPlocR];
+    const float4 alo = s_lo[threadIdx.x + R], ahi = s_hi[threadIdx.x + R];
     unsigned long long best = ~0ull;
-    for (int d = -kPlocR; d <= kPlocR; ++d) {
+    for (int d = -R; d <= R; ++d) {
         const int j = i + d;
         if (d == 0 || j < 0 || j >= (int)m) continue;
-        const float4 blo = s_lo[threadIdx.x + kPlocR + d], bhi = s_hi[threadIdx.x + kPlocR + d];
+        const float4 blo = s_lo[threadIdx.x + R + d], bhi = s_hi[threadIdx.x + R + d];
         const float4 ulo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.0f);
         const float4 uhi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.0f);
         const unsigned long long key =
@@ -824,7 +833,7 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
             e = cudaErrorUnknown;
             goto done;
         }
-        k_ploc_nn<<<blocks(m), kBB, 0, s>>>(cl, m, nlo, nhi, nn);
+        k_ploc_nn<<<blocks(m), kBB, 0, s>>>(cl, m, nlo, nhi, nn, g_ploc_radius);
         k_ploc_flags<<<blocks(m), kBB, 0, s>>>(nn, m, flags);
         count_launch();
         count_launch();

@@ -31,5 +31,8 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
                                bool want8, cudaStream_t s, DeviceBuild* out);
 
 cudaError_t status_build(uint32_t* out);
+// PLOC search radius, 1..64 clusters on either side (default 8).
+void set_ploc_radius(int r);
+int get_ploc_radius();
 
 }  // namespace wfpt
