@@ -46,12 +46,13 @@ COURTYARD = dict(
 # Shadow rays are generated in the (already reordered) slot order of their
 # path rays and all aim at the light, so the chosen form does not sort them.
 # The chosen form replays each frame as one captured graph with persistent
-# BVH8 traversal; the plain form launches every stage directly (unbatched)
-# with FP32 BVH2 nodes.
+# BVH8 traversal, each pass's shadow rays traced on a second stream while
+# the next bounce runs; the plain form launches every stage directly on one
+# stream (unbatched) with FP32 BVH2 nodes.
 CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=0,
-              reorder_shadow_rays=0, use_graph=1)
+              reorder_shadow_rays=0, use_graph=1, shadow_overlap=1)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
-             reorder_shadow_rays=0, use_graph=0)
+             reorder_shadow_rays=0, use_graph=0, shadow_overlap=0)
 # Per-bounce reordering mask chosen by autotune.tune_bounce_sort on this
 # workload (bench.py --sweep): every bounce traces unsorted.
 TUNED_PATH_SORT_SKIP = 0xFF

@@ -447,7 +447,8 @@ typedef struct wfpt_renderer wfpt_renderer;
 
 /* Renderer options; keys and defaults follow the reference's env options
  * (Environment/AppEnvironment.cpp:10-43, Renderer.cpp:300-308) plus the
- * additions morton_kind, bvh_kind, albedo, use_graph. */
+ * additions morton_kind, bvh_kind, albedo, use_graph, path_sort_skip,
+ * shadow_overlap. */
 typedef struct wfpt_renderer_config {
     int ray_type;                   /* Renderer.rayType */
     int num_primary_samples;        /* Renderer.numberOfPrimarySamples, 1..1024 */
@@ -468,6 +469,12 @@ typedef struct wfpt_renderer_config {
     int path_sort_skip;             /* bit b set: bounce b+1 traces its path rays
                                        unsorted even when sort_path_rays is on
                                        (per-bounce reordering; 0..255, default 0) */
+    int shadow_overlap;             /* 1 (default): each pass's shadow rays are
+                                       traced and reconstructed on a second
+                                       stream while the next bounce's path rays
+                                       are generated, sorted and traced; 0: one
+                                       stream in the reference's order.  Results
+                                       are identical. */
 } wfpt_renderer_config;
 
 void wfpt_renderer_config_default(wfpt_renderer_config* config);

@@ -97,6 +97,10 @@ class same_bits:
          num_shadow_samples=3),
     # per-bounce reordering: bounces 1 and 3 unsorted, 2 and 4 sorted + reordered
     dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, path_sort_skip=0b0101),
+    # shadow passes on the frame's stream in the reference's order (the
+    # other cases overlap them with the next bounce)
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, shadow_overlap=0),
+    dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1, shadow_overlap=0),
 ])
 def test_path_frame_bit_exact(wf, orc, dev, small, opts):
     px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 96, 64, **opts)
@@ -131,6 +135,9 @@ def test_accumulation_over_frames_and_spp(wf, orc, dev, small):
     dict(),
     dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1),
     dict(ray_type=1, sort_shadow_rays=1, reorder_shadow_rays=1),
+    dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1, morton_kind=2,
+         bvh_kind=1, num_primary_samples=2),
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, shadow_overlap=0),
 ])
 def test_graph_frames_match_direct_frames(wf, dev, small, opts):
     """use_graph=1 replays one captured frame with the camera and frame

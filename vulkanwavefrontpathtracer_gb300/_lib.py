@@ -69,6 +69,7 @@ class RendererConfig(C.Structure):
         ("albedo", c_float),
         ("use_graph", c_int),
         ("path_sort_skip", c_int),
+        ("shadow_overlap", c_int),
     ]
 
 

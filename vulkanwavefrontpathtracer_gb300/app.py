@@ -15,6 +15,8 @@ Options beyond the reference (same file, same style):
   Renderer.useGraph       bool                         (default true)
   Renderer.pathSortSkip   int bit mask: bit b set = bounce b+1 traces its
                           path rays unsorted (per-bounce reordering, default 0)
+  Renderer.shadowOverlap  bool: trace each pass's shadow rays concurrently with
+                          the next bounce (default true; same image)
   Benchmark.warmupCycles  int                          (default 3)
   Benchmark.benchmarkCycles int                        (default 10)
   Scene.generator         "soup:<triangles>:<seed>" | "courtyard[:<seed>]" |
@@ -68,6 +70,7 @@ DEFAULTS: Dict[str, Any] = {
     "Renderer.albedo": 0.8,
     "Renderer.useGraph": True,
     "Renderer.pathSortSkip": 0,
+    "Renderer.shadowOverlap": True,
     "Camera.position": [0.0, 0.0, 0.0],
     "Camera.rotation": [0.0, 0.0, 0.0],
     "Camera.nearPlane": 0.001,
@@ -158,7 +161,8 @@ def renderer_config(opts: Dict[str, Any]):
         bvh_kind=BVH_KINDS[opts["Renderer.bvh"]],
         albedo=opts["Renderer.albedo"],
         use_graph=1 if opts["Renderer.useGraph"] else 0,
-        path_sort_skip=opts["Renderer.pathSortSkip"])
+        path_sort_skip=opts["Renderer.pathSortSkip"],
+        shadow_overlap=1 if opts["Renderer.shadowOverlap"] else 0)
 
 
 # ------------------------------------------------------------ scene input

@@ -104,6 +104,14 @@ struct wfpt_renderer {
     // one stream, one after another), so that renderers running
     // concurrently never share one.
     DevBuf work;
+    // Shadow-pass overlap (cfg.shadow_overlap): the shadow rays of a pass
+    // are traced and reconstructed on `side` while the next bounce runs on
+    // the frame's stream; that branch has its own work counters, sort
+    // scratch and colour buffer (aux2 alternates with aux per pass).
+    DevBuf aux2, work_side, sort_scratch_side;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool shadow_pending = false;
     RayBufferDev primary, shadow, queue[2];
     uint32_t* host_counters = nullptr;  // pinned
     int last_spp = 0;
@@ -193,7 +201,11 @@ struct wfpt_renderer {
         if (graph) cudaGraphDestroy(graph);
         if (fp_dev) cudaFree(fp_dev);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters, &work})
+        if (side) cudaStreamDestroy(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters, &work, &aux2,
+                        &work_side, &sort_scratch_side})
             b->release();
         primary.release();
         shadow.release();
@@ -269,6 +281,19 @@ struct wfpt_renderer {
             if ((e = work.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
             if ((e = cudaMemset(work.p, 0, work.bytes)) != cudaSuccess) return e;
         }
+        if (cfg.shadow_overlap) {
+            if ((e = aux2.ensure(n * 16)) != cudaSuccess) return e;
+            if (!work_side.p) {
+                if ((e = work_side.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
+                if ((e = cudaMemset(work_side.p, 0, work_side.bytes)) != cudaSuccess) return e;
+            }
+            if (cfg.sort_shadow_rays &&
+                (e = sort_scratch_side.ensure(wfpt::sort_scratch_bytes((uint32_t)shadow_cap, 64))) != cudaSuccess)
+                return e;
+            if (!side && (e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking)) != cudaSuccess) return e;
+            if (!ev_fork && (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+            if (!ev_join && (e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)) != cudaSuccess) return e;
+        }
         if (!host_counters &&
             (e = cudaMallocHost(&host_counters, (size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess)
             return e;
@@ -278,19 +303,22 @@ struct wfpt_renderer {
         return cudaSuccess;
     }
 
-    // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).
+    // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).  on_side: the
+    // launch belongs to the shadow branch (its own counters and scratch).
     cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool on_side = false) {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
+        uint32_t* wk = on_side ? work_side.as<uint32_t>() : work.as<uint32_t>();
+        DevBuf& scratch = on_side ? sort_scratch_side : sort_scratch;
         cudaError_t e;
         if (!sort) return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
-                                             n_dev, closest ? 1 : 0, s, work.as<uint32_t>());
+                                             n_dev, closest ? 1 : 0, s, wk);
         float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
         if ((e = wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
                                      rb.idx.as<uint32_t>(), s)) != cudaSuccess)
             return e;
-        if ((e = wfpt::launch_sort_pairs(rb.keys.p, rb.idx.as<uint32_t>(), n, n_dev, key_bits(), sort_scratch.p,
-                                         sort_scratch.bytes, s)) != cudaSuccess)
+        if ((e = wfpt::launch_sort_pairs(rb.keys.p, rb.idx.as<uint32_t>(), n, n_dev, key_bits(), scratch.p,
+                                         scratch.bytes, s)) != cudaSuccess)
             return e;
         if (reorder) {
             if ((e = wfpt::launch_reorder(rb.idx.as<uint32_t>(), rb.rays_cur(), rb.rays_out(), rb.s2i_cur(),
@@ -299,13 +327,24 @@ struct wfpt_renderer {
             rb.swap();
         }
         return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
-                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s,
-                                  work.as<uint32_t>());
+                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s, wk);
+    }
+
+    // Makes stream s wait for the shadow branch forked last (if any).
+    cudaError_t join_shadow(cudaStream_t s) {
+        if (!shadow_pending) return cudaSuccess;
+        shadow_pending = false;
+        return cudaStreamWaitEvent(s, ev_join, 0);
     }
 
     // Renderer::shadowPass (Renderer.cpp:133-154) over input rays `in`
     // whose slot->pixel map is `in_s2i`; n_in is the capacity, n_in_dev the
-    // device-side count (null when the host count is exact).
+    // device-side count (null when the host count is exact).  With
+    // shadow_overlap and a single batch, the shadow rays are generated on s
+    // (raygenShadow reads the seeds that the next raygenPath rewrites) and
+    // traced, reconstructed and counted on the side stream; join_shadow()
+    // waits for that branch before the next shadow pass, which keeps the
+    // order of the additions into out_pixels.
     cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
                             const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
                             uint32_t* batch_counter, cudaStream_t s) {
@@ -313,6 +352,32 @@ struct wfpt_renderer {
         uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
         uint32_t bb = 0;
         cudaError_t e;
+        if ((e = join_shadow(s)) != cudaSuccess) return e;
+        if (cfg.shadow_overlap && side && n_in <= batch_diff) {
+            const uint32_t* n_sh_dev = nullptr;
+            if (n_in_dev) {
+                if ((e = wfpt::launch_batch_count(n_in_dev, 0, n_in, S, batch_counter, s)) != cudaSuccess) return e;
+                n_sh_dev = batch_counter;
+            }
+            shadow.swapped = false;
+            if ((e = wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, shadow.rays_cur(),
+                                                shadow.s2i_cur(), shadow.i2s_cur(), light, cfg.shadow_radius, 0,
+                                                (int)n_in, n_in_dev, S, s)) != cudaSuccess)
+                return e;
+            if ((e = cudaEventRecord(ev_fork, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
+            if ((e = trace_rays(shadow, n_in * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
+                                cfg.reorder_shadow_rays != 0, false, side, true)) != cudaSuccess)
+                return e;
+            if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
+                                                     in_pixels, out_pixels, 0, (int)n_in, n_in_dev, S, 0, side)) !=
+                cudaSuccess)
+                return e;
+            if ((e = wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, side)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
+            shadow_pending = true;
+            return cudaSuccess;
+        }
         do {
             uint32_t be = std::min(bb + batch_diff, n_in);
             uint32_t bs = be - bb;
@@ -382,17 +447,23 @@ struct wfpt_renderer {
                 if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp)) != cudaSuccess) return e;
                 continue;
             }
-            // renderShadow / renderPath (Renderer.cpp:168-199).
-            if ((e = cudaMemsetAsync(aux.p, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
-            if ((e = primary_pass(s2w, eye, zfar, pass, aux.as<float>(), s, fp)) != cudaSuccess) return e;
+            // renderShadow / renderPath (Renderer.cpp:168-199).  Colour
+            // buffers alternate between passes when shadow passes overlap
+            // the next bounce (one is still read by the pending shadow pass).
+            float* auxb[2] = {aux.as<float>(), cfg.shadow_overlap ? aux2.as<float>() : aux.as<float>()};
+            int ai = 0;
+            if ((e = join_shadow(s)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+            if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp)) != cudaSuccess) return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
-                                 aux.as<float>(), frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s)) !=
+                                 auxb[ai], frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s)) !=
                 cudaSuccess)
                 return e;
             if (rt != WFPT_PATH_RAYS) continue;
             int qsel = 0;  // PathQueue::swapBuffers
             for (int bounce = 0; bounce < cfg.recursion_depth; ++bounce) {
-                if ((e = cudaMemsetAsync(aux.p, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
+                ai ^= 1;
+                if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
                 RayBufferDev& out = queue[qsel ? 0 : 1];
                 const wfpt_ray* in_rays;
                 const wfpt_hit* in_res;
@@ -422,16 +493,17 @@ struct wfpt_renderer {
                     cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
-                                                         aux.as<float>(), decreases.as<float>(), geoms, light, bg, n,
+                                                         auxb[ai], decreases.as<float>(), geoms, light, bg, n,
                                                          out_cnt, cfg.num_primary_samples, s)) != cudaSuccess)
                     return e;
                 if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
-                                     aux.as<float>(), frame_pixels, cnt(pass, kCntHits + bounce + 1),
+                                     auxb[ai], frame_pixels, cnt(pass, kCntHits + bounce + 1),
                                      cnt(pass, kCntBatch), s)) != cudaSuccess)
                     return e;
                 qsel ^= 1;  // PathQueue::swap
             }
         }
+        if ((e = join_shadow(s)) != cudaSuccess) return e;
         return wfpt::launch_interpolate_colors(frame_pixels, pixels, n, frame_index, cfg.key_value, cfg.white_point, s,
                                                fp);
     }
@@ -450,6 +522,7 @@ wfpt_status check_config(const wfpt_renderer_config* c) {
     if (c->morton_kind < WFPT_MORTON_AILA32 || c->morton_kind > WFPT_MORTON_6D64) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->bvh_kind != WFPT_BVH2_FP32 && c->bvh_kind != WFPT_BVH8_Q8) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->path_sort_skip < 0 || c->path_sort_skip > 255) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->shadow_overlap < 0 || c->shadow_overlap > 1) return WFPT_ERR_INVALID_ARGUMENT;
     return WFPT_OK;
 }
 
@@ -479,6 +552,7 @@ void wfpt_renderer_config_default(wfpt_renderer_config* c) {
     c->albedo = 0.8f;
     c->use_graph = 0;
     c->path_sort_skip = 0;
+    c->shadow_overlap = 1;
 }
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config, wfpt_renderer** renderer) {
