@@ -60,11 +60,11 @@ WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 b
                  "chosen form = BVH8-Q8 + 64-bit 6-D Morton keys + sort/reorder of path rays")
 METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s vs peak"
 # DRAM bytes (read + write) per ray of the full-size bounce-1 BVH8 traversal
-# launches (2,073,600 closest-hit path rays, 4,147,200 any-hit shadow rays),
-# median of 12 launches each from one ncu capture of
+# launches (2,073,600 sorted closest-hit path rays, 4,147,200 any-hit shadow
+# rays), median of 12 launches each from one ncu capture of
 # `bench.py --micro-only` (dram__bytes_read.sum + dram__bytes_write.sum,
-# cold caches): closest 88.9 MB + 10.9 MB, any-hit 154.3 MB + 41.0 MB.
-TRACE_DRAM_BYTES_PER_RAY = {"any": 47.08, "closest": 48.13}
+# cold caches): closest 87.6 MB + 10.2 MB, any-hit 152.9 MB + 40.6 MB.
+TRACE_DRAM_BYTES_PER_RAY = {"any": 46.64, "closest": 47.20}
 
 
 def peaks():
