@@ -804,11 +804,24 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")
     ap.add_argument("--sort-micro", action="store_true", help="sort/reorder microbenchmark over --sort-sizes")
     ap.add_argument("--sort-sizes", default="65536,262144,1048576,2073600,4194304,16777216,67108864")
+    ap.add_argument("--scene-build", action="store_true",
+                    help="acceleration-structure build times only (host vs device; courtyard and city)")
     ap.add_argument("--batched", action="store_true", help="the 64-request batched serving workload")
     ap.add_argument("--batch-requests", type=int, default=64)
     args = ap.parse_args()
     if args.batched:
         run_batched(args)
+        return
+    if args.scene_build:
+        import torch
+
+        import vulkanwavefrontpathtracer_gb300 as wf
+        from vulkanwavefrontpathtracer_gb300 import build as wbuild
+        wbuild.build()
+        torch.cuda.set_device(0)
+        W = COURTYARD
+        pos, nrm, idx = wf.api.generate_scene(W["scene_kind"], W["seed"])
+        print(json.dumps({"scene_build": scene_build_times(wf.api, pos, idx, wf.api.Scene(pos, idx))}))
         return
     if args.sweep:
         run_sweep(args)

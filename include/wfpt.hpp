@@ -168,9 +168,24 @@ public:
         check(wfpt_scene_create(positions, num_vertices, indices, num_triangles, geometry_first_triangle,
                                 num_geometries, bvh_kinds_mask, &s_));
     }
+    /* Geometry already in device memory: both BVHs built on the GPU
+     * (wfpt_scene_create_device). */
+    static Scene fromDevice(const float* positions_dev, uint32_t num_vertices, const uint32_t* indices_dev,
+                            uint32_t num_triangles, const uint32_t* geometry_first_triangle = nullptr,
+                            uint32_t num_geometries = 0,
+                            int bvh_kinds_mask = (1 << WFPT_BVH2_FP32) | (1 << WFPT_BVH8_Q8),
+                            cudaStream_t stream = nullptr) {
+        wfpt_scene* s = nullptr;
+        check(wfpt_scene_create_device(positions_dev, num_vertices, indices_dev, num_triangles,
+                                       geometry_first_triangle, num_geometries, bvh_kinds_mask, stream, &s));
+        return Scene(s);
+    }
+    Scene(Scene&& o) noexcept : s_(o.s_) { o.s_ = nullptr; }
     Scene(const Scene&) = delete;
     Scene& operator=(const Scene&) = delete;
-    ~Scene() { wfpt_scene_destroy(s_); }
+    ~Scene() {
+        if (s_) wfpt_scene_destroy(s_);
+    }
     const wfpt_scene* get() const { return s_; }
     wfpt_scene_info info() const {
         wfpt_scene_info i;
@@ -179,6 +194,7 @@ public:
     }
 
 private:
+    explicit Scene(wfpt_scene* s) : s_(s) {}
     wfpt_scene* s_ = nullptr;
 };
 

@@ -2,8 +2,10 @@
 // would use it.  `facade_test host` needs no GPU: errors surface as
 // wfpt_cxx::Error and a host-only scene builds.  `facade_test gpu` runs
 // RayGen::primary, Tracer::trace and Tracer::traceSort (with and without
-// reordering) and RayGen::shadow on a seeded triangle soup, checking that
-// traceSort returns the same hits as trace.  Prints "FACADE OK" on success.
+// reordering), a scene built on the device from device buffers, and
+// RayGen::shadow on a seeded triangle soup, checking that traceSort and the
+// device-built scene return the same hits as trace.  Prints "FACADE OK" on
+// success.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -107,6 +109,28 @@ static int gpu_mode() {
                 if (std::memcmp(&re[i], &plain[order[i]], sizeof(wfpt_hit)) != 0)
                     return fail("reordered traceSort differs from trace");
         }
+    }
+    // The same mesh with both BVHs built on the GPU gives the same hits.
+    {
+        DeviceArray<float> dpos;
+        DeviceArray<uint32_t> didx;
+        dpos.resize(pos.size());
+        didx.resize(idx.size());
+        check_cuda(cudaMemcpy(dpos.get(), pos.data(), pos.size() * 4, cudaMemcpyHostToDevice));
+        check_cuda(cudaMemcpy(didx.get(), idx.data(), idx.size() * 4, cudaMemcpyHostToDevice));
+        Scene dscene = Scene::fromDevice(dpos.get(), (uint32_t)(pos.size() / 3), didx.get(), 20000);
+        if (dscene.info().num_triangles != 20000) return fail("device-built scene info");
+        tracer.setAccelerationStructure(scene, WFPT_BVH8_Q8);
+        rays.setClosestHit(true);
+        tracer.trace(rays);
+        const std::vector<wfpt_hit> host_hits = to_host(rays.getResultBuffer(), (size_t)n);
+        tracer.setAccelerationStructure(dscene, WFPT_BVH8_Q8);
+        tracer.trace(rays);
+        const std::vector<wfpt_hit> dev_hits = to_host(rays.getResultBuffer(), (size_t)n);
+        // dscene ends with this block: the tracer must not keep it.
+        tracer.setAccelerationStructure(scene, WFPT_BVH8_Q8);
+        if (std::memcmp(host_hits.data(), dev_hits.data(), (size_t)n * sizeof(wfpt_hit)) != 0)
+            return fail("device-built scene hits differ");
     }
     // Shadow rays of the primary hits, traced any-hit.
     RayBuffer shadow;

@@ -115,14 +115,29 @@ __global__ void __launch_bounds__(kBB) k_tri_bounds(const float* __restrict__ po
         ch[k] = __reduce_max_sync(0xffffffffu, ch[k]);
     }
     pm = __reduce_max_sync(0xffffffffu, pm);
+    // Block reduction of the 13 values (one atomic per value and block:
+    // per-warp atomics on the same 13 words serialised on 3M triangles).
+    __shared__ uint32_t s_red[kBB / 32][13];
+    const uint32_t warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
-            atomicMin(&st->bmin[k], bl[k]);
-            atomicMax(&st->bmax[k], bh[k]);
-            atomicMin(&st->cmin[k], cl[k]);
-            atomicMax(&st->cmax[k], ch[k]);
+            s_red[warp][k] = bl[k];
+            s_red[warp][3 + k] = bh[k];
+            s_red[warp][6 + k] = cl[k];
+            s_red[warp][9 + k] = ch[k];
         }
-        atomicMax(&st->pmax, pm);
+        s_red[warp][12] = pm;
+    }
+    __syncthreads();
+    if (threadIdx.x < 13) {
+        const uint32_t q = threadIdx.x;
+        const bool is_min = q < 3 || (q >= 6 && q < 9);
+        uint32_t v = s_red[0][q];
+        for (int w = 1; w < kBB / 32; ++w) v = is_min ? min(v, s_red[w][q]) : max(v, s_red[w][q]);
+        uint32_t* dst = q < 3 ? &st->bmin[q] : q < 6 ? &st->bmax[q - 3] : q < 9 ? &st->cmin[q - 6]
+                      : q < 12 ? &st->cmax[q - 9] : &st->pmax;
+        if (is_min) atomicMin(dst, v);
+        else atomicMax(dst, v);
     }
 }
 
