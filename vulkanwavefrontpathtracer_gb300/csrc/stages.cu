@@ -246,33 +246,48 @@ constexpr uint32_t kValueMask = (1u << 30) - 1u;
 
 // Exclusive prefix of `count` over tiles 0..tile-1 by decoupled look-back.
 // Called by every thread of the block; returns the prefix in all threads.
+// Warp 0 reads 32 predecessors per round trip (lane k: tile - 1 - k), finds
+// the nearest one that published its inclusive prefix, and sums the values
+// down to it; a window with an unpublished entry before that is re-read
+// (bounded: kSpinLimit rounds, then kErrTimeout).
 __device__ uint32_t tile_prefix(uint32_t* tile_state, uint32_t tile, uint32_t count) {
     __shared__ uint32_t s_prefix;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+        const uint32_t lane = threadIdx.x;
         if (tile == 0) {
-            atomicExch(&tile_state[0], kFlagPrefix | count);
-            s_prefix = 0;
+            if (lane == 0) {
+                atomicExch(&tile_state[0], kFlagPrefix | count);
+                s_prefix = 0;
+            }
         } else {
-            atomicExch(&tile_state[tile], kFlagAggregate | count);
-            uint32_t excl = 0;
-            int32_t j = (int32_t)tile - 1;
-            uint32_t spins = 0;
-            while (j >= 0) {
-                uint32_t st = *((volatile uint32_t*)&tile_state[j]);
-                uint32_t flag = st & ~kValueMask;
-                if (flag == 0u) {
+            if (lane == 0) atomicExch(&tile_state[tile], kFlagAggregate | count);
+            uint32_t excl = 0, spins = 0;
+            int32_t top = (int32_t)tile - 1;
+            for (;;) {
+                const int32_t t = top - (int32_t)lane;
+                // Below tile 0: a virtual inclusive prefix of 0.
+                uint32_t st = kFlagPrefix;
+                if (t >= 0) st = *((volatile uint32_t*)&tile_state[t]);
+                const uint32_t flag = st & ~kValueMask;
+                const uint32_t pref = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+                const uint32_t unset = __ballot_sync(0xffffffffu, flag == 0u);
+                const uint32_t p = pref ? (uint32_t)__ffs(pref) - 1u : 32u;
+                const uint32_t upto = p < 31u ? ((2u << p) - 1u) : 0xffffffffu;  // lanes 0..p
+                if (unset & upto) {
                     if (++spins > kSpinLimit) {
                         raise_status(kErrTimeout);
                         break;
                     }
                     continue;
                 }
-                excl += st & kValueMask;
-                if (flag == kFlagPrefix) break;
-                --j;
+                excl += __reduce_add_sync(0xffffffffu, lane <= p ? (st & kValueMask) : 0u);
+                if (p < 32u) break;
+                top -= 32;
             }
-            atomicExch(&tile_state[tile], kFlagPrefix | (excl + count));
-            s_prefix = excl;
+            if (lane == 0) {
+                atomicExch(&tile_state[tile], kFlagPrefix | (excl + count));
+                s_prefix = excl;
+            }
         }
     }
     __syncthreads();
