@@ -139,11 +139,25 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          for a nearest neighbour (1..64, default 8)
  *   "build.bvh8.tri_cost"  triangle-test cost relative to a node step in the
  *                          SAH collapse, percent (1..10000, default 20)
+ *   "debug.fail_alloc_after"  fault injection: n >= 0 makes the renderer's
+ *                          device allocation after n more successful ones
+ *                          report WFPT_ERR_OUT_OF_MEMORY (nothing is
+ *                          allocated); -1 (default) off
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */
 wfpt_status wfpt_tune_set(const char* key, int64_t value);
 wfpt_status wfpt_tune_get(const char* key, int64_t* value);
+/* Self-test of the device-side failure detection (no reference counterpart;
+ * the reference waits on fences and asserts).  Runs one bounded device wait
+ * that cannot succeed -- which = 0: a radix sort pass whose decoupled
+ * look-back waits on a tile that nothing publishes; 1: the path-ray
+ * compaction's look-back likewise -- and returns what wfpt_device_status
+ * then reports: WFPT_ERR_TIMEOUT when the wait gave up as designed (the
+ * status word is cleared and the context stays usable).  Synchronises the
+ * device; takes one to a few seconds. */
+wfpt_status wfpt_selftest_wait_timeout(int which);
+
 /* Counters of the counting traversal kernels (synchronises): out[0] node
  * visits, out[1] triangle tests, out[2] rays, out[3] persistent-warp loop
  * iterations; reset != 0 zeroes them. */

@@ -53,6 +53,7 @@ def test_invalid_arguments_rejected_on_host(wf):
     assert b"aligned" in lib.wfpt_last_error_message()
     assert lib.wfpt_reorder_records(buf, buf, buf, 48, None, None, None, 4, None, None) == 1  # in place
     assert lib.wfpt_reorder_records(None, None, None, 48, None, None, None, 0, None, None) == 0  # empty
+    assert lib.wfpt_selftest_wait_timeout(2) == 1  # no such self-test
     out = C.c_void_p()
     assert lib.wfpt_scene_create_device(None, 3, None, 5, None, 0, 3, None, C.byref(out)) == 1  # null mesh
     assert lib.wfpt_scene_create_device(buf, 3, buf, 5, None, 0, 3 | 0x100, None, C.byref(out)) == 1  # host-only
@@ -305,7 +306,8 @@ def test_tuning_knobs(wf):
         assert api.tune_get("trace.bvh8.coop") == 0
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
                          ("trace.bvh8.coop", 2), ("sort.tiles", 4), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("build.bvh8.collapse", 2),
-                         ("build.bvh8.tri_cost", 0), ("build.bvh8.tri_cost", 10001), ("no.such.knob", 1)):
+                         ("build.bvh8.tri_cost", 0), ("build.bvh8.tri_cost", 10001), ("build.ploc.radius", 0),
+                         ("build.ploc.radius", 65), ("debug.fail_alloc_after", -2), ("no.such.knob", 1)):
             with pytest.raises(wf.WfptError):
                 api.tune_set(key, bad)
     finally:

@@ -139,6 +139,7 @@ _SIGS = {
     "wfpt_sort_scratch_bytes": (c_size_t, [c_u32, c_int]),
     "wfpt_sort_pairs": (c_int, [c_void_p, c_void_p, c_u32, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "wfpt_reorder": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_void_p, c_void_p]),
+    "wfpt_selftest_wait_timeout": (c_int, [c_int]),
     "wfpt_reorder_records": (c_int, [c_void_p, c_void_p, c_void_p, c_u32, c_void_p, c_void_p, c_void_p, c_u32, c_void_p,
                                      c_void_p]),
     "wfpt_raygen_shadow": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, P_f32, c_float, c_int,

@@ -56,6 +56,14 @@ def tune_set(key: str, value: int) -> None:
     L.check(lib().wfpt_tune_set(key.encode(), int(value)))
 
 
+def selftest_wait_timeout(which: int) -> int:
+    """Runs one bounded device wait that cannot succeed (0: radix sort
+    look-back, 1: path compaction look-back) and returns the wfpt_status
+    that wfpt_device_status reports afterwards (WFPT_ERR_TIMEOUT = 4 when
+    the wait gave up as designed)."""
+    return int(lib().wfpt_selftest_wait_timeout(int(which)))
+
+
 def tune_get(key: str) -> int:
     v = C.c_int64(0)
     L.check(lib().wfpt_tune_get(key.encode(), C.byref(v)))

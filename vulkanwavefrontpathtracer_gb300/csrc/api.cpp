@@ -115,6 +115,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_sort_digit_bits((int)value);
         return WFPT_OK;
     }
+    if (k == "debug.fail_alloc_after") {
+        if (value < -1 || value > (1 << 20)) return invalid("debug.fail_alloc_after must be in [-1, 2^20]");
+        wfpt::set_fail_alloc_after((int)value);
+        return WFPT_OK;
+    }
     if (k == "build.ploc.radius") {
         if (value < 1 || value > 64) return invalid("build.ploc.radius must be in [1, 64]");
         wfpt::set_ploc_radius((int)value);
@@ -168,6 +173,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
         *value = wfpt::get_sort_digit_bits();
         return WFPT_OK;
     }
+    if (k == "debug.fail_alloc_after") {
+        *value = wfpt::get_fail_alloc_after();
+        return WFPT_OK;
+    }
     if (k == "build.ploc.radius") {
         *value = wfpt::get_ploc_radius();
         return WFPT_OK;
@@ -205,6 +214,22 @@ wfpt_status wfpt_device_status(uint32_t* flags) {
         return WFPT_ERR_DEVICE_BOUNDS;
     }
     return WFPT_OK;
+}
+
+wfpt_status wfpt_selftest_wait_timeout(int which) {
+    if (which != 0 && which != 1) return invalid("which must be 0 (radix sort) or 1 (path compaction)");
+    cudaError_t e = cudaDeviceSynchronize();
+    uint32_t before = 0;
+    if (e == cudaSuccess) e = wfpt::status_stages(&before);
+    if (e == cudaSuccess) e = wfpt::status_sort(&before);
+    if (e != cudaSuccess) return from_cuda(e);
+    if (before) {
+        g_last_error = "device status was already set before the self-test";
+        return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    e = which == 0 ? wfpt::sort_selftest_timeout(nullptr) : wfpt::raygen_path_selftest_timeout(nullptr);
+    if (e != cudaSuccess) return from_cuda(e);
+    return wfpt_device_status(nullptr);
 }
 
 wfpt_status wfpt_pixel_table(int width, int height, int32_t* index_to_pixel, int32_t* pixel_to_index) {

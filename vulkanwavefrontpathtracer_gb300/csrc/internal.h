@@ -20,4 +20,8 @@ const SceneDevice* scene_device(const wfpt_scene* s);
 bool scene_has(const wfpt_scene* s, int kind);
 void scene_bounds(const wfpt_scene* s, float mn[3], float mx[3]);
 
+// Renderer allocation fault injection (renderer.cpp).
+void set_fail_alloc_after(int n);
+int get_fail_alloc_after();
+
 }  // namespace wfpt

@@ -12,6 +12,7 @@
 //  - buffers are sized once per resolution (capacity = width*height rays per
 //    wavefront) and the frame can be captured into one CUDA graph;
 //  - ray statistics are read back once, after the frame.
+#include <atomic>
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -33,6 +34,11 @@ constexpr int kCountersPerPass = 32;
 // the input rays of each shadow pass, [17] shadow rays of the current batch.
 constexpr int kCntPath = 0, kCntHits = 8, kCntBatch = 17;
 
+// Fault injection (knob "debug.fail_alloc_after"): when >= 0, the renderer's
+// allocation after that many more succeeds reports out of memory, without
+// touching the device.  -1 = off.
+static std::atomic<int> g_fail_alloc_after{-1};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -41,6 +47,10 @@ struct DevBuf {
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
+        int left = g_fail_alloc_after.load();
+        while (left >= 0 && !g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {
+        }
+        if (left == 0) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&p, b);
         if (e == cudaSuccess) bytes = b;
         return e;
@@ -508,6 +518,11 @@ struct wfpt_renderer {
                                                fp);
     }
 };
+
+namespace wfpt {
+void set_fail_alloc_after(int n) { g_fail_alloc_after = n < 0 ? -1 : n; }
+int get_fail_alloc_after() { return g_fail_alloc_after; }
+}  // namespace wfpt
 
 namespace {
 

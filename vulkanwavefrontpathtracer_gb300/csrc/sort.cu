@@ -500,6 +500,40 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     return sort_passes<K, xlarge, 8>(keys, values, n, n_dev, key_bits, L, scratch, s);
 }
 
+// Failure-detection self-test: one pass of a two-tile 32-bit sort run by a
+// single CTA that draws ticket 1, so its look-back waits on tile 0, which
+// nothing publishes.  The wait gives up after kSpinLimit polls and latches
+// kErrTimeout; the scatter that follows writes only in-bounds slots (its
+// positions are checked against the count).  Synchronises the stream.
+cudaError_t sort_selftest_timeout(cudaStream_t s) {
+    constexpr int KPT = kKptSmall32;
+    constexpr uint32_t TILE = kSortThreads * KPT, N = 2 * TILE;
+    cudaError_t e = sort_prepare();
+    if (e != cudaSuccess) return e;
+    uint32_t* buf = nullptr;  // keys, values, keys out, values out, ticket, lookback
+    const size_t words = 4 * (size_t)N + 1 + 2 * kRadix;
+    if ((e = cudaMalloc(&buf, words * sizeof(uint32_t))) != cudaSuccess) return e;
+    uint32_t* keys = buf;
+    uint32_t* vals = keys + N;
+    uint32_t* keys_out = vals + N;
+    uint32_t* vals_out = keys_out + N;
+    uint32_t* ticket = vals_out + N;
+    uint32_t* lookback = ticket + 1;
+    const uint32_t one = 1;
+    e = cudaMemsetAsync(buf, 0, words * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ticket, &one, sizeof(one), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        k_onesweep<uint32_t, KPT, 8><<<1, kSortThreads, onesweep_smem<uint32_t, KPT, 8>(), s>>>(
+            keys, vals, keys_out, vals_out, N, nullptr, 0, 0xFFu, lookback /* unused for tile 1 */, lookback,
+            ticket, 0);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(buf);
+    return e != cudaSuccess ? e : e2;
+}
+
 cudaError_t launch_sort_pairs(void* keys, uint32_t* values, uint32_t n, const uint32_t* n_dev, int key_bits,
                               void* scratch, size_t scratch_bytes, cudaStream_t s) {
     (void)scratch_bytes;

@@ -579,6 +579,44 @@ cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, cons
     return cudaGetLastError();
 }
 
+// Failure-detection self-test: the path compaction over two 256-ray tiles
+// of misses, run by a single block that draws ticket 1, so its look-back
+// waits on tile 0, which nothing publishes; the wait gives up after
+// kSpinLimit rounds and latches kErrTimeout.  All rays miss, so nothing but
+// the count is written.  Synchronises the stream.
+cudaError_t raygen_path_selftest_timeout(cudaStream_t s) {
+    constexpr uint32_t N = 2 * kBlock;
+    // seeds, i2p in/out, count, scratch (ticket + 2 tile states) as words;
+    // rays in/out, results, decreases as 16-byte records.
+    const size_t words = 3 * (size_t)N + 1 + 3;
+    const size_t vec4s = 2 * (size_t)N * 2 + N + N;
+    unsigned char* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, vec4s * 16 + words * 4);
+    if (e != cudaSuccess) return e;
+    float4* in_rays = reinterpret_cast<float4*>(buf);
+    float4* out_rays = in_rays + 2 * N;
+    int4* results = reinterpret_cast<int4*>(out_rays + 2 * N);
+    float4* decreases = reinterpret_cast<float4*>(results + N);
+    uint32_t* seeds = reinterpret_cast<uint32_t*>(decreases + N);
+    int32_t* in_i2p = reinterpret_cast<int32_t*>(seeds + N);
+    int32_t* out_i2p = in_i2p + N;
+    uint32_t* count = reinterpret_cast<uint32_t*>(out_i2p + N);
+    uint32_t* scratch = count + 1;
+    const uint32_t one = 1;
+    e = cudaMemsetAsync(buf, 0, vec4s * 16 + words * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(results, 0xFF, N * sizeof(int4), s);  // every ray a miss
+    if (e == cudaSuccess) e = cudaMemcpyAsync(scratch, &one, sizeof(one), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        k_raygen_path<<<1, kBlock, 0, s>>>(seeds, nullptr, in_rays, out_rays, in_i2p, out_i2p, results, decreases,
+                                           count, N, nullptr, 0.8f, scratch);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(buf);
+    return e != cudaSuccess ? e : e2;
+}
+
 // Library-owned compaction scratch for launch_raygen_path_static: the tile
 // ticket (word 0) and one look-back state per 256-ray tile (words 1..),
 // for at most WFPT_RAYGEN_PATH_STATIC_MAX_RAYS rays; 65,537 words (256 KiB)

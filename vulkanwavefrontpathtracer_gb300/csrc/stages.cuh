@@ -27,6 +27,10 @@ uint64_t launch_count();
 cudaError_t status_stages(uint32_t* out);
 cudaError_t status_sort(uint32_t* out);
 cudaError_t status_trace(uint32_t* out);
+// Failure-detection self-tests (one bounded device wait that cannot
+// succeed; see sort.cu / stages.cu).
+cudaError_t sort_selftest_timeout(cudaStream_t s);
+cudaError_t raygen_path_selftest_timeout(cudaStream_t s);
 
 cudaError_t launch_init_seeds(uint32_t* seeds, uint32_t n, int frame, cudaStream_t s,
                               const FrameParams* fp = nullptr);
