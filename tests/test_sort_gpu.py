@@ -126,7 +126,7 @@ def test_sort_scratch_too_small(wf, dev):
 @pytest.mark.parametrize("n,key_bits", [(1, 32), (2047, 32), (2049, 32), (4095, 32), (4097, 32), (8191, 32),
                                         (8193, 32), (10239, 32), (10241, 32), (123457, 32), (9000, 12),
                                         (70001, 33), (1535, 63), (1537, 64), (3073, 63), (7167, 63), (7169, 63),
-                                        (14337, 64), (300001, 48), (65537, 62), (2073600, 63)])
+                                        (14337, 64), (7679, 63), (7681, 63), (15361, 64), (300001, 48), (65537, 62), (2073600, 63)])
 def test_sort_tile_variants(wf, dev, tiles, n, key_bits, digit_bits):
     """Every tile size and both digit widths give the stable order, at sizes
     around the tile boundaries, odd and even pass counts, key widths that

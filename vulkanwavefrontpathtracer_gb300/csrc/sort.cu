@@ -43,12 +43,14 @@ constexpr uint32_t kLbPrefix = 2u << 30;
 constexpr uint32_t kLbValue = (1u << 30) - 1u;
 constexpr int kLbChunk = 16;  // predecessors read per look-back round trip
 
-// Keys per thread of the tile variants (tile = 512 * KPT keys).  32-bit
-// keys have a third, extra-large variant for sorts of many waves (10 %
-// faster than 16 keys per thread on 2^26 keys); for 64-bit keys the large
-// tile is already the largest that leaves room for two CTAs per SM.
+// Keys per thread of the tile variants (tile = 512 * KPT keys).  The
+// extra-large variant serves sorts of more than two waves of large tiles:
+// 20 keys per thread for 32-bit keys (10 % faster than 16 on 2^26 keys).
+// For 64-bit keys it is the large tile (15 keys per thread measured 2-4 %
+// slower on 2^24-2^26 keys; 14 is close to the most that leaves room for
+// two CTAs per SM).
 constexpr int kKptSmall32 = 8, kKptLarge32 = 16, kKptXLarge32 = 20;
-constexpr int kKptSmall64 = 8, kKptLarge64 = 14;
+constexpr int kKptSmall64 = 8, kKptLarge64 = 14, kKptXLarge64 = kKptLarge64;
 
 // Digit mask of pass p with db-bit digits: the top pass keeps only the
 // bits below key_bits.
@@ -382,7 +384,7 @@ cudaError_t sort_prepare() {
 }
 
 // Tile variant: 0 = automatic, 1 = small, 2 = large, 3 = extra-large tiles
-// (64-bit keys: same as large).  Automatic takes the small tiles while they
+// (64-bit keys: the large ones).  Automatic takes the small tiles while they
 // fit in one wave (two tiles per SM), the large ones while those fit in two
 // waves (a frame-sized sort), and the extra-large ones beyond.
 static int g_sort_tiles = 0;
@@ -488,7 +490,7 @@ static cudaError_t sort_impl(K* keys, uint32_t* values, uint32_t n, const uint32
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     constexpr bool wide = sizeof(K) == 8;
     constexpr int small = wide ? kKptSmall64 : kKptSmall32, large = wide ? kKptLarge64 : kKptLarge32;
-    constexpr int xlarge = wide ? kKptLarge64 : kKptXLarge32;
+    constexpr int xlarge = wide ? kKptXLarge64 : kKptXLarge32;
     const int tv = tile_variant(n, wide);
     if (g_digit_bits == 4) {
         if (tv == 1) return sort_passes<K, small, 4>(keys, values, n, n_dev, key_bits, L, scratch, s);
