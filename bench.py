@@ -224,7 +224,10 @@ def run_ours(args):
     tune = autotune.tune_bounce_sort(lambda m: make(dict(CHOSEN, path_sort_skip=m)), cam, w, h,
                                      W["renderer"]["recursion_depth"], frames=3, device=dev)
     mask = int(tune["path_sort_skip"])
-    tuned = make(dict(CHOSEN, path_sort_skip=mask))
+    ptune = autotune.tune_primary_bvh(lambda k: make(dict(CHOSEN, path_sort_skip=mask, primary_bvh_kind=k)), cam, w,
+                                      h, frames=3, device=dev)
+    pkind = int(ptune["primary_bvh_kind"])
+    tuned = make(dict(CHOSEN, path_sort_skip=mask, primary_bvh_kind=pkind))
     ms_t, rays_t, _, _ = timed_frames(tuned, args.steps, max(1, args.warmup // 2))
     tuned_value = rays_t / (ms_t * 1e-3) / 1e6
 
@@ -284,10 +287,15 @@ def run_ours(args):
             "chosen_over_plain": round(value / plain_value, 3),
             "autotuned": {"value": round(tuned_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_t / args.steps, 4),
                           "over_plain": round(tuned_value / plain_value, 3), "path_sort_skip": mask,
+                          "primary_bvh_kind": pkind,
                           "search": [{"path_sort_skip": e["path_sort_skip"], "ms": round(e["ms"], 3)}
-                                     for e in tune["table"]],
-                          "note": "chosen form with the per-bounce reordering picked live by "
-                                  "autotune.tune_bounce_sort (bit b set: bounce b+1 unsorted)"},
+                                     for e in tune["table"]]
+                          + [{"primary_bvh_kind": e["primary_bvh_kind"], "ms": round(e["ms"], 3)}
+                             for e in ptune["table"]],
+                          "note": "chosen form with the per-bounce reordering (autotune.tune_bounce_sort; bit b "
+                                  "set: bounce b+1 unsorted) and the primary pass's BVH (tune_primary_bvh; 0 = "
+                                  "FP32 BVH2 for the coherent camera rays) picked live; incoherent bounces use "
+                                  "the BVH8"},
             "per_bounce": micro["per_bounce"],
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),

@@ -462,7 +462,7 @@ typedef struct wfpt_renderer wfpt_renderer;
 /* Renderer options; keys and defaults follow the reference's env options
  * (Environment/AppEnvironment.cpp:10-43, Renderer.cpp:300-308) plus the
  * additions morton_kind, bvh_kind, albedo, use_graph, path_sort_skip,
- * shadow_overlap. */
+ * shadow_overlap, primary_bvh_kind. */
 typedef struct wfpt_renderer_config {
     int ray_type;                   /* Renderer.rayType */
     int num_primary_samples;        /* Renderer.numberOfPrimarySamples, 1..1024 */
@@ -489,6 +489,11 @@ typedef struct wfpt_renderer_config {
                                        are generated, sorted and traced; 0: one
                                        stream in the reference's order.  Results
                                        are identical. */
+    int primary_bvh_kind;           /* BVH traversed by the primary pass (camera
+                                       rays and their shadow rays): -1 (default)
+                                       = bvh_kind, else a wfpt_bvh_kind.  On
+                                       coherent camera rays the FP32 BVH2 is the
+                                       faster one (the autotuner's choice). */
 } wfpt_renderer_config;
 
 void wfpt_renderer_config_default(wfpt_renderer_config* config);

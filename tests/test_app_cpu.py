@@ -42,9 +42,13 @@ def test_env_options_and_defaults(app):
     assert (cfg.sort_shadow_rays, cfg.reorder_shadow_rays, cfg.sort_path_rays, cfg.reorder_path_rays) == (1, 0, 1, 1)
     assert (cfg.morton_kind, cfg.bvh_kind) == (2, 1)
     assert abs(cfg.shadow_radius - 0.5) < 1e-7
+    assert cfg.primary_bvh_kind == -1 and cfg.shadow_overlap == 1
+    o2 = app.load_env(dict(ENV, Renderer=dict(ENV["Renderer"], primaryBvh="bvh2")))
+    assert app.renderer_config(o2).primary_bvh_kind == 0
 
 
 @pytest.mark.parametrize("bad", [{"Renderer": {"rayType": "photon"}}, {"Renderer": {"numberOfBounces": 3}},
+                                 {"Renderer": {"primaryBvh": "bvh4"}},
                                  {"Camera": {"position": "1 2"}}, {"Nope": {"x": 1}}])
 def test_env_rejects_bad_options(app, bad):
     with pytest.raises(ValueError):

@@ -101,6 +101,9 @@ class same_bits:
     # other cases overlap them with the next bounce)
     dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, shadow_overlap=0),
     dict(sort_path_rays=1, reorder_path_rays=1, sort_shadow_rays=1, reorder_shadow_rays=1, shadow_overlap=0),
+    # the primary pass on the other BVH than the bounces
+    dict(sort_path_rays=1, reorder_path_rays=1, morton_kind=2, bvh_kind=1, primary_bvh_kind=0),
+    dict(bvh_kind=0, primary_bvh_kind=1),
 ])
 def test_path_frame_bit_exact(wf, orc, dev, small, opts):
     px, fp, st, o_px, o_fp, o_st = run_pair(wf, orc, dev, small, 96, 64, **opts)
@@ -166,3 +169,23 @@ def test_graph_frames_match_direct_frames(wf, dev, small, opts):
     for (pa, fa, na, sa), (pb, fb, nb, sb) in zip(*outs):
         assert na == nb and sa == sb
         assert same_bits(pa, pb) and same_bits(fa, fb)
+
+
+def test_renderer_rejects_missing_bvh_kind(wf, dev):
+    """A renderer whose primary pass (or bounces) asks for a BVH the scene
+    was built without is refused at set_scene and at render, before any
+    traversal launch."""
+    import torch
+    pos, nrm, idx = wf.api.generate_scene(0, 6, 2000)
+    only8 = wf.api.Scene(pos, idx, bvh2=False)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    r = wf.api.Renderer(ray_type=wf.PATH_RAYS, bvh_kind=wf.BVH8_Q8, primary_bvh_kind=wf.BVH2_FP32)
+    with pytest.raises(wf.WfptError):
+        r.set_scene(only8, geom, LIGHT, BG)
+    r2 = wf.api.Renderer(ray_type=wf.PATH_RAYS, bvh_kind=wf.BVH8_Q8)
+    r2.set_scene(only8, geom, LIGHT, BG)
+    r2.set_config(wf.api.default_config(ray_type=wf.PATH_RAYS, bvh_kind=wf.BVH8_Q8, primary_bvh_kind=wf.BVH2_FP32))
+    px = torch.zeros((16 * 16, 4), dtype=torch.float32, device=dev)
+    with pytest.raises(wf.WfptError):
+        r2.render(wf.api.make_camera(**CAM), 16, 16, px, px.clone())
+    assert wf.api.device_status() == 0

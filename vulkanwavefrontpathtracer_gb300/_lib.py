@@ -70,6 +70,7 @@ class RendererConfig(C.Structure):
         ("use_graph", c_int),
         ("path_sort_skip", c_int),
         ("shadow_overlap", c_int),
+        ("primary_bvh_kind", c_int),
     ]
 
 

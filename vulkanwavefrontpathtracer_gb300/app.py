@@ -15,6 +15,8 @@ Options beyond the reference (same file, same style):
   Renderer.useGraph       bool                         (default true)
   Renderer.pathSortSkip   int bit mask: bit b set = bounce b+1 traces its
                           path rays unsorted (per-bounce reordering, default 0)
+  Renderer.primaryBvh     "bvh2" | "bvh8" | "" (default: Renderer.bvh): BVH of the
+                          primary pass (camera rays and their shadow rays)
   Renderer.shadowOverlap  bool: trace each pass's shadow rays concurrently with
                           the next bounce (default true; same image)
   Benchmark.warmupCycles  int                          (default 3)
@@ -71,6 +73,7 @@ DEFAULTS: Dict[str, Any] = {
     "Renderer.useGraph": True,
     "Renderer.pathSortSkip": 0,
     "Renderer.shadowOverlap": True,
+    "Renderer.primaryBvh": "",
     "Camera.position": [0.0, 0.0, 0.0],
     "Camera.rotation": [0.0, 0.0, 0.0],
     "Camera.nearPlane": 0.001,
@@ -136,7 +139,7 @@ def load_env(source) -> Dict[str, Any]:
     if unknown:
         raise ValueError(f"unknown options: {', '.join(sorted(unknown))}")
     for key, table in (("Renderer.rayType", RAY_TYPES), ("Renderer.mortonKind", MORTON_KINDS),
-                       ("Renderer.bvh", BVH_KINDS)):
+                       ("Renderer.bvh", BVH_KINDS), ("Renderer.primaryBvh", dict(BVH_KINDS, **{"": -1}))):
         if opts[key] not in table:
             raise ValueError(f"{key} must be one of {sorted(table)}")
     return opts
@@ -162,7 +165,8 @@ def renderer_config(opts: Dict[str, Any]):
         albedo=opts["Renderer.albedo"],
         use_graph=1 if opts["Renderer.useGraph"] else 0,
         path_sort_skip=opts["Renderer.pathSortSkip"],
-        shadow_overlap=1 if opts["Renderer.shadowOverlap"] else 0)
+        shadow_overlap=1 if opts["Renderer.shadowOverlap"] else 0,
+        primary_bvh_kind=-1 if opts["Renderer.primaryBvh"] == "" else BVH_KINDS[opts["Renderer.primaryBvh"]])
 
 
 # ------------------------------------------------------------ scene input

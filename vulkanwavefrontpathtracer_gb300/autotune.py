@@ -168,6 +168,31 @@ def tune_bounce_sort(make_renderer, camera, width: int, height: int, depth: int,
     return {"path_sort_skip": best_mask, "ms": best_ms, "table": table}
 
 
+def tune_primary_bvh(make_renderer, camera, width: int, height: int, frames: int = 3, device=None) -> Dict:
+    """BVH of the primary pass (coherent camera rays and their shadow
+    rays): make_renderer(primary_bvh_kind) returns a renderer with its scene
+    set; whole frames are timed with the FP32 BVH2 and with the BVH8 there.
+    Returns the faster kind and the table (median ms of `frames` frames)."""
+    import statistics
+
+    import torch
+    dev = device or torch.device("cuda", 0)
+    px = torch.zeros((width * height, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+    table = []
+    for kind in (L.BVH2_FP32, L.BVH8_Q8):
+        r = make_renderer(kind)
+        r.render(camera, width, height, px, fp)
+        times = []
+        for _ in range(frames):
+            r.render(camera, width, height, px, fp)
+            times.append(r.stats().frame_ms)
+        r.close()
+        table.append({"primary_bvh_kind": kind, "ms": statistics.median(times)})
+    best = min(table, key=lambda e: e["ms"])
+    return {"primary_bvh_kind": best["primary_bvh_kind"], "ms": best["ms"], "table": table}
+
+
 def measure_work(scene: api.Scene, rays, bvh_kind: int, closest: bool) -> Dict:
     """Node visits and triangle tests per ray (counting kernel variants)."""
     import torch

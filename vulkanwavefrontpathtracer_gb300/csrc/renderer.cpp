@@ -316,12 +316,12 @@ struct wfpt_renderer {
     // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).  on_side: the
     // launch belongs to the shadow branch (its own counters and scratch).
     cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
-                           cudaStream_t s, bool on_side = false) {
+                           cudaStream_t s, bool on_side, int kind) {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
         uint32_t* wk = on_side ? work_side.as<uint32_t>() : work.as<uint32_t>();
         DevBuf& scratch = on_side ? sort_scratch_side : sort_scratch;
         cudaError_t e;
-        if (!sort) return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
+        if (!sort) return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
                                              n_dev, closest ? 1 : 0, s, wk);
         float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
         if ((e = wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
@@ -336,9 +336,11 @@ struct wfpt_renderer {
                 return e;
             rb.swap();
         }
-        return wfpt::launch_trace(sc, cfg.bvh_kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
+        return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
                                   reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s, wk);
     }
+
+    int primary_kind() const { return cfg.primary_bvh_kind >= 0 ? cfg.primary_bvh_kind : cfg.bvh_kind; }
 
     // Makes stream s wait for the shadow branch forked last (if any).
     cudaError_t join_shadow(cudaStream_t s) {
@@ -357,7 +359,7 @@ struct wfpt_renderer {
     // order of the additions into out_pixels.
     cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
                             const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
-                            uint32_t* batch_counter, cudaStream_t s) {
+                            uint32_t* batch_counter, cudaStream_t s, int kind) {
         int S = cfg.num_shadow_samples;
         uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
         uint32_t bb = 0;
@@ -377,7 +379,7 @@ struct wfpt_renderer {
             if ((e = cudaEventRecord(ev_fork, s)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
             if ((e = trace_rays(shadow, n_in * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
-                                cfg.reorder_shadow_rays != 0, false, side, true)) != cudaSuccess)
+                                cfg.reorder_shadow_rays != 0, false, side, true, kind)) != cudaSuccess)
                 return e;
             if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
                                                      in_pixels, out_pixels, 0, (int)n_in, n_in_dev, S, 0, side)) !=
@@ -402,7 +404,7 @@ struct wfpt_renderer {
                                                 (int)bs, n_in_dev, S, s)) != cudaSuccess)
                 return e;
             if ((e = trace_rays(shadow, bs * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
-                                cfg.reorder_shadow_rays != 0, false, s)) != cudaSuccess)
+                                cfg.reorder_shadow_rays != 0, false, s, false, kind)) != cudaSuccess)
                 return e;
             if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
                                                      in_pixels, out_pixels, (int)bb, (int)bs, n_in_dev, S, 0, s)) !=
@@ -422,7 +424,7 @@ struct wfpt_renderer {
         if ((e = wfpt::launch_raygen_primary(s2w, i2p.as<int32_t>(), primary.rays_cur(), eye, sample_index, width,
                                              height, zfar, s, fp, pass, cfg.num_primary_samples)) != cudaSuccess)
             return e;
-        if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), cfg.bvh_kind, primary.rays_cur(),
+        if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), primary_kind(), primary.rays_cur(),
                                     primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s,
                                     work.as<uint32_t>())) != cudaSuccess)
             return e;
@@ -466,8 +468,8 @@ struct wfpt_renderer {
             if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
             if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp)) != cudaSuccess) return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
-                                 auxb[ai], frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s)) !=
-                cudaSuccess)
+                                 auxb[ai], frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s,
+                                 primary_kind())) != cudaSuccess)
                 return e;
             if (rt != WFPT_PATH_RAYS) continue;
             int qsel = 0;  // PathQueue::swapBuffers
@@ -499,7 +501,8 @@ struct wfpt_renderer {
                                                   cfg.albedo, path_scratch.p, s)) != cudaSuccess)
                     return e;
                 const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
-                if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s)) !=
+                if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s, false,
+                                    cfg.bvh_kind)) !=
                     cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
@@ -508,7 +511,7 @@ struct wfpt_renderer {
                     return e;
                 if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
                                      auxb[ai], frame_pixels, cnt(pass, kCntHits + bounce + 1),
-                                     cnt(pass, kCntBatch), s)) != cudaSuccess)
+                                     cnt(pass, kCntBatch), s, cfg.bvh_kind)) != cudaSuccess)
                     return e;
                 qsel ^= 1;  // PathQueue::swap
             }
@@ -538,6 +541,8 @@ wfpt_status check_config(const wfpt_renderer_config* c) {
     if (c->bvh_kind != WFPT_BVH2_FP32 && c->bvh_kind != WFPT_BVH8_Q8) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->path_sort_skip < 0 || c->path_sort_skip > 255) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->shadow_overlap < 0 || c->shadow_overlap > 1) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->primary_bvh_kind != -1 && c->primary_bvh_kind != WFPT_BVH2_FP32 && c->primary_bvh_kind != WFPT_BVH8_Q8)
+        return WFPT_ERR_INVALID_ARGUMENT;
     return WFPT_OK;
 }
 
@@ -568,6 +573,7 @@ void wfpt_renderer_config_default(wfpt_renderer_config* c) {
     c->use_graph = 0;
     c->path_sort_skip = 0;
     c->shadow_overlap = 1;
+    c->primary_bvh_kind = -1;
 }
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config, wfpt_renderer** renderer) {
@@ -607,7 +613,7 @@ wfpt_status wfpt_renderer_set_scene(wfpt_renderer* r, const wfpt_scene* scene, c
                                     const float scene_min[3], const float scene_max[3], const float light[3],
                                     const float background[3]) {
     if (!r || !scene || !geometries) return WFPT_ERR_INVALID_ARGUMENT;
-    if (!wfpt::scene_has(scene, r->cfg.bvh_kind)) {
+    if (!wfpt::scene_has(scene, r->cfg.bvh_kind) || !wfpt::scene_has(scene, r->primary_kind())) {
         wfpt::set_error("scene was built without the renderer's BVH kind");
         return WFPT_ERR_UNSUPPORTED;
     }
@@ -634,6 +640,10 @@ wfpt_status wfpt_renderer_render(wfpt_renderer* r, const wfpt_camera* camera, in
     if (!r->scene) {
         wfpt::set_error("renderer has no scene");
         return WFPT_ERR_INVALID_ARGUMENT;
+    }
+    if (!wfpt::scene_has(r->scene, r->cfg.bvh_kind) || !wfpt::scene_has(r->scene, r->primary_kind())) {
+        wfpt::set_error("scene was built without the renderer's BVH kind");
+        return WFPT_ERR_UNSUPPORTED;
     }
     if (width <= 0 || height <= 0 || (long long)width * height > (1ll << 28)) {
         wfpt::set_error("bad resolution");
@@ -782,7 +792,8 @@ wfpt_status wfpt_batch_create(const wfpt_request* requests, uint32_t count, int 
             wfpt::set_error("request option out of range");
             return WFPT_ERR_INVALID_ARGUMENT;
         }
-        if (!wfpt::scene_has(q.scene, q.config.bvh_kind)) {
+        if (!wfpt::scene_has(q.scene, q.config.bvh_kind) ||
+            (q.config.primary_bvh_kind >= 0 && !wfpt::scene_has(q.scene, q.config.primary_bvh_kind))) {
             wfpt::set_error("request scene was built without the request's BVH kind");
             return WFPT_ERR_UNSUPPORTED;
         }

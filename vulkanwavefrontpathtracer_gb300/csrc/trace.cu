@@ -807,6 +807,9 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
                          const uint32_t* ray_index, uint32_t n, const uint32_t* n_dev, int closest,
                          cudaStream_t s, uint32_t* own_work) {
     if (n == 0) return cudaSuccess;
+    // A scene built without this BVH kind has no buffers for it.
+    if (kind == WFPT_BVH8_Q8 ? (!sc.bvh8_nodes || !sc.bvh8_tris) : (!sc.bvh2_nodes || !sc.bvh2_tris))
+        return cudaErrorInvalidValue;
     unsigned grid = (n + kBlock - 1) / kBlock;
     const float4* rr = reinterpret_cast<const float4*>(rays);
     int4* out = reinterpret_cast<int4*>(results);
