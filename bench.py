@@ -53,6 +53,15 @@ CHOSEN = dict(bvh_kind=1, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, 
               reorder_shadow_rays=0, use_graph=1, shadow_overlap=1)
 PLAIN = dict(bvh_kind=0, morton_kind=0, sort_path_rays=0, reorder_path_rays=0, sort_shadow_rays=0,
              reorder_shadow_rays=0, use_graph=0, shadow_overlap=0)
+# The city block (3,000,320 triangles; its BVH2 does not fit in L2) at
+# 3840x2160: the per-bounce comparison on the largest incoherent workload.
+CITY = dict(
+    scene_kind=2, seed=1, width=3840, height=2160,
+    camera=dict(position=(320.0, 90.0, 700.0), rotation_deg=(-25.0, 0.0, 0.0), fov_deg=60.0, znear=0.1,
+                zfar=2048.0),
+    light=(320.0, 300.0, 320.0), background=(0.529, 0.808, 0.98),
+    renderer=dict(num_shadow_samples=2, shadow_radius=4.0),
+)
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + persistent graph-captured wavefront + 64-bit 6-D Morton sort/reorder "
                  "of the path rays of every bounce")
@@ -128,25 +137,47 @@ def setup_dist():
 
 
 # ------------------------------------------------------------------ ours
-def scene_build_times(api, pos, idx, host_scene):
+def city_bounce(wf, api, dev, stream):
+    """The bounce-1 comparison of `bounce_micro` on the city block at
+    3840x2160 (8.3M primary rays).  Returns its per-bounce line and the
+    host-built city scene (for the build-time report)."""
+    W = CITY
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx)
+    geom = api.Geometry(pos, nrm, idx, device=dev)
+    cam = api.make_camera(**W["camera"])
+    micro = bounce_micro(wf, api, dev, scene, geom, cam, W["width"], W["height"], stream, workload=W)
+    line = dict(micro["per_bounce"])
+    line["triangles"] = int(scene.info.num_triangles)
+    line["resolution"] = [W["width"], W["height"]]
+    line["sort_gbs"] = round(micro["sort"]["gbs"], 1)
+    del geom
+    return line, (pos, idx, scene)
+
+
+def scene_build_times(api, pos, idx, host_scene, city=None):
     """Acceleration-structure build times (BVH2 + BVH8) of the courtyard and
     the 3M-triangle city block: host build (binned SAH + collapse) and device
     build (PLOC + collapse on the GPU; the first device build of the process
-    also loads the build kernels, so it is done once untimed)."""
+    also loads the build kernels, so it is done once untimed).  `city`: the
+    city's (positions, indices, host-built scene), when already built."""
     out = {"courtyard_host_ms": round(host_scene.info.build_ms, 1)}
     warm = api.Scene(pos, idx, device_build=True)
     warm.close()
     d = api.Scene(pos, idx, device_build=True)
     out["courtyard_device_ms"] = round(d.info.build_ms, 1)
     d.close()
-    cpos, _, cidx = api.generate_scene(2, 1)
+    if city is None:
+        cpos, _, cidx = api.generate_scene(2, 1)
+        hsc = api.Scene(cpos, cidx)
+    else:
+        cpos, cidx, hsc = city
+    out["city_host_ms"] = round(hsc.info.build_ms, 1)
+    hsc.close()
     d = api.Scene(cpos, cidx, device_build=True)
     out["city_triangles"] = int(d.info.num_triangles)
     out["city_device_ms"] = round(d.info.build_ms, 1)
     d.close()
-    hsc = api.Scene(cpos, cidx)
-    out["city_host_ms"] = round(hsc.info.build_ms, 1)
-    hsc.close()
     out["city_device_speedup"] = round(out["city_host_ms"] / max(out["city_device_ms"], 1e-3), 1)
     out["note"] = "device-built trees trace the courtyard's bounce-1 rays 10-13 % slower (PLOC vs binned SAH)"
     return out
@@ -252,7 +283,11 @@ def run_ours(args):
     micro = bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream)
     hbm, peak_kind = peaks()
     out = None
-    builds = scene_build_times(api, pos, idx, scene) if rank == 0 else None
+    builds = city_line = None
+    if rank == 0:
+        city_line, city = city_bounce(wf, api, dev, stream)
+        builds = scene_build_times(api, pos, idx, scene, city=city)
+        del city
     if rank == 0:
         cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
         if cpu is not None:
@@ -297,6 +332,7 @@ def run_ours(args):
                                   "FP32 BVH2 for the coherent camera rays) picked live; incoherent bounces use "
                                   "the BVH8"},
             "per_bounce": micro["per_bounce"],
+            "per_bounce_city": city_line,
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),
                              "reorder_frac": round(micro["reorder"]["gbs"] / hbm, 3)},
@@ -316,10 +352,11 @@ def run_ours(args):
     return out
 
 
-def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
+def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream, workload=None):
     """One incoherent bounce: primary hits -> cosine bounce rays (bounce 1),
     then traced plain (BVH2, unsorted) and chosen (6-D keys, sort, reorder,
     BVH8).  Also times the sort and reorder kernels alone."""
+    W = workload or COURTYARD
     import torch
     n = w * h
     i2p_np, _ = api.pixel_table(w, h)
@@ -380,13 +417,12 @@ def bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream):
     ms_trace2_sorted = timeit(lambda: api.trace(scene, wf.BVH2_FP32, out, res))
     # The bounce's shadow rays (2 per path ray, toward the area light): the
     # any-hit traversal that takes the largest share of a frame.
-    S = COURTYARD["renderer"]["num_shadow_samples"]
+    S = W["renderer"]["num_shadow_samples"]
     srays = torch.empty((S * m, 8), dtype=torch.float32, device=dev)
     ss2i = torch.empty(S * m, dtype=torch.int32, device=dev)
     si2s = torch.empty(S * m, dtype=torch.int32, device=dev)
     sres = torch.empty((S * m, 4), dtype=torch.int32, device=dev)
-    api.raygen_shadow(seeds, out, res, srays, ss2i, si2s, COURTYARD["light"], COURTYARD["renderer"]["shadow_radius"],
-                      0, m, S)
+    api.raygen_shadow(seeds, out, res, srays, ss2i, si2s, W["light"], W["renderer"]["shadow_radius"], 0, m, S)
     ms_shadow8 = timeit(lambda: api.trace(scene, wf.BVH8_Q8, srays, sres, closest_hit=False))
     ms_shadow2 = timeit(lambda: api.trace(scene, wf.BVH2_FP32, srays, sres, closest_hit=False))
     ms_sort = timeit(lambda: api.sort_pairs(keys, ids, 63, scratch=scratch))
@@ -494,6 +530,10 @@ def run_micro_only(args):
     wbuild.build()
     dev = torch.device("cuda", 0)
     api = wf.api
+    if args.city:
+        line, _ = city_bounce(wf, api, dev, torch.cuda.current_stream())
+        print(json.dumps({"per_bounce_city": line}))
+        return
     W = COURTYARD
     pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
     scene = api.Scene(pos, idx)
@@ -814,6 +854,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--micro-only", action="store_true",
                     help="only the bounce-1 microbenchmark (small profiling case with --width/--height)")
+    ap.add_argument("--city", action="store_true",
+                    help="with --micro-only: the bounce-1 comparison on the city block at 3840x2160")
     ap.add_argument("--width", type=int, default=COURTYARD["width"])
     ap.add_argument("--height", type=int, default=COURTYARD["height"])
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")

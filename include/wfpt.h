@@ -121,13 +121,17 @@ uint64_t wfpt_kernel_launch_count(void);
  * autotuner).  Keys:
  *   "trace.bvh8.refill"    refill a persistent warp when this many lanes
  *                          are idle (1..32, default 8)
- *   "trace.bvh8.postpone"  postpone a node's triangle tests while fewer than
- *                          this many lanes have triangles (0..32, 0 = off)
+ *   "trace.bvh8.postpone"  per-lane triangle tests (coop 0): postpone a
+ *                          node's triangle tests while fewer than this many
+ *                          lanes have triangles (0..32, 0 = off)
  *   "trace.bvh8.coop"      1 = the warp tests all of its lanes' pending
  *                          triangles together, 32 at a time (default);
  *                          0 = each lane tests its own.  Closest hits are
  *                          identical; an any-hit ray may report a different
  *                          (equally valid) occluder
+ *   "trace.bvh8.batch"     cooperative tests: run them once this many are
+ *                          pending across the warp's node steps (1..32,
+ *                          default 24; 1 = after every node step)
  *   "sort.tiles"           radix sort tile size: 0 = by problem size
  *                          (default), 1 = small tiles, 2 = large tiles,
  *                          3 = extra-large tiles (32-bit keys; 64-bit keys

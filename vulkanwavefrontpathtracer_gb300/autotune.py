@@ -36,32 +36,39 @@ def _timeit(fn: Callable[[], None], reps: int = 5, warm: int = 2) -> float:
 
 
 def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[int] = (1, 2, 4, 8, 16, 32),
-                   postpones: Iterable[int] = (0, 4, 8, 12), coops: Iterable[int] = (0, 1), reps: int = 5) -> Dict:
-    """Grid search of (refill, postpone, coop) for BVH8 closest-hit and
-    any-hit traversal; returns the best settings and the full table (ms)."""
+                   postpones: Iterable[int] = (0, 4, 8, 12), coops: Iterable[int] = (0, 1),
+                   batches: Iterable[int] = (1, 8, 16, 24, 32), reps: int = 5) -> Dict:
+    """Grid search of refill x (cooperative tests: batch; per-lane tests:
+    postpone) for BVH8 closest-hit and any-hit traversal; returns the best
+    settings and the full table (ms)."""
     import torch
     dev = closest_rays.device
     res_c = torch.empty((closest_rays.shape[0], 4), dtype=torch.int32, device=dev)
     res_a = torch.empty((any_rays.shape[0], 4), dtype=torch.int32, device=dev)
-    old = (api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"), api.tune_get("trace.bvh8.coop"))
+    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch")
+    old = [api.tune_get(k) for k in keys]
+    grid = []
+    for coop in coops:
+        for refill in refills:
+            for v in (batches if coop else postpones):
+                grid.append((refill, 0 if coop else v, coop, v if coop else old[3]))
     table = []
     try:
-        for refill, post, coop in itertools.product(refills, postpones, coops):
-            api.tune_set("trace.bvh8.refill", refill)
-            api.tune_set("trace.bvh8.postpone", post)
-            api.tune_set("trace.bvh8.coop", coop)
+        for refill, post, coop, batch in grid:
+            for k, v in zip(keys, (refill, post, coop, batch)):
+                api.tune_set(k, v)
             mc = _timeit(lambda: api.trace(scene, L.BVH8_Q8, closest_rays, res_c, closest_hit=True), reps)
             ma = _timeit(lambda: api.trace(scene, L.BVH8_Q8, any_rays, res_a, closest_hit=False), reps)
-            table.append({"refill": refill, "postpone": post, "coop": coop, "closest_ms": mc, "any_ms": ma})
+            table.append({"refill": refill, "postpone": post, "coop": coop, "batch": batch, "closest_ms": mc,
+                          "any_ms": ma})
     finally:
-        api.tune_set("trace.bvh8.refill", old[0])
-        api.tune_set("trace.bvh8.postpone", old[1])
-        api.tune_set("trace.bvh8.coop", old[2])
+        for k, v in zip(keys, old):
+            api.tune_set(k, v)
     # The knobs are shared by both kinds of rays: weigh them by ray count.
     nc, na = closest_rays.shape[0], any_rays.shape[0]
     best = min(table, key=lambda e: e["closest_ms"] + e["any_ms"])
-    return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "table": table,
-            "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
+    return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "batch": best["batch"],
+            "table": table, "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
             "best_any_mrays_s": na / (best["any_ms"] * 1e-3) / 1e6}
 
 
@@ -219,3 +226,5 @@ def apply(traversal: Dict) -> None:
     api.tune_set("trace.bvh8.postpone", traversal["postpone"])
     if "coop" in traversal:
         api.tune_set("trace.bvh8.coop", traversal["coop"])
+    if "batch" in traversal:
+        api.tune_set("trace.bvh8.batch", traversal["batch"])

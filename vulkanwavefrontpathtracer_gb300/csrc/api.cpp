@@ -99,6 +99,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_trace_postpone((uint32_t)value);
         return WFPT_OK;
     }
+    if (k == "trace.bvh8.batch") {
+        if (value < 1 || value > 32) return invalid("trace.bvh8.batch must be in [1, 32]");
+        wfpt::set_trace_batch((uint32_t)value);
+        return WFPT_OK;
+    }
     if (k == "trace.bvh8.coop") {
         if (value < 0 || value > 1) return invalid("trace.bvh8.coop must be 0 or 1");
         wfpt::set_trace_coop(value != 0);
@@ -159,6 +164,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "trace.bvh8.postpone") {
         *value = wfpt::get_trace_postpone();
+        return WFPT_OK;
+    }
+    if (k == "trace.bvh8.batch") {
+        *value = (int64_t)wfpt::get_trace_batch();
         return WFPT_OK;
     }
     if (k == "trace.bvh8.coop") {

@@ -573,22 +573,31 @@ __device__ __forceinline__ void write_hit_key(int4* __restrict__ results, uint32
 }
 
 constexpr uint32_t kRecBits = 27;  // task word: lane << 27 | triangle record
-constexpr int kTaskCap = 32 * 24;  // a node hands a lane at most 24 triangles
+constexpr int kRing = 1024;        // per-warp ring of pending triangle tests (power of two)
 
 // Same traversal as k_trace_bvh8, except that triangle tests are shared by
-// the warp: after each node step every lane lists its (lane, triangle)
-// pairs in shared memory and the warp tests the list 32 pairs at a time,
+// the warp: each node step appends its lanes' (lane, triangle) pairs to a
+// ring in shared memory, and the warp tests the ring 32 pairs at a time,
 // each result folded into the owner's best hit key with a shared atomicMin.
-// Any-hit rays report the nearest hit of the first list that has one.
+// Tests are batched across node steps: the ring is tested once `batch` or
+// more pairs are pending (in whole passes of 32 when 32 or more are), and
+// entirely once the lanes waiting on their own tests plus the idle lanes
+// would fill a refill, or no lane has nodes left.  A lane's ray finishes
+// only when its traversal is exhausted (any hit: when it has a hit) and all
+// of its own tests have run, so a ring entry never outlives its ray.  The
+// deferred tests leave tcur larger for a few node steps (culling stays
+// conservative: tcur only shrinks), which costs about 1 % more node steps
+// and saves most of the partly empty test passes (batch 1: test every
+// step).  At most 31 + 32 * 24 pairs are pending after an append.
 template <bool CLOSEST, bool COUNT>
 __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
     const float4* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
     int4* __restrict__ results, const uint32_t* __restrict__ ray_index, uint32_t n,
     const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ rec_of_key, uint32_t* __restrict__ work,
-    uint32_t refill, uint32_t postpone) {
+    uint32_t refill, uint32_t batch) {
     __shared__ RayS s_ray[kBlock];
     __shared__ unsigned long long s_best[kBlock];
-    __shared__ uint32_t s_task[kBlock / 32][kTaskCap];
+    __shared__ uint32_t s_task[kBlock / 32][kRing];
     const uint32_t count = load_count(n, n_dev);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -603,6 +612,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
     RayT r;
     float tcur = 0.0f;
     uint2 ng = make_uint2(0u, 0u);
+    // Ring counters (absolute, wrapped by the ring mask; equal in all
+    // lanes): pairs [tested, appended) are pending.  my_end: one past this
+    // lane's last appended pair.
+    uint32_t tested = 0, appended = 0, my_end = 0;
     uint32_t c_nodes = 0, c_tris = 0, c_rays = 0, c_iters = 0;
     for (;;) {
         bool want = state != kTracing && !exhausted;
@@ -639,45 +652,33 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
                     exhausted = true;
                 }
             }
+            want_mask = 0u;  // refilled (or out of rays)
         }
-        const uint32_t busy = __ballot_sync(0xffffffffu, state == kTracing);
         if (__ballot_sync(0xffffffffu, state != kIdle || !exhausted) == 0u) break;
         if (COUNT && lane == 0) ++c_iters;
 
         uint32_t tri_base = 0, tg = 0;
-        if (state == kTracing) {
+        if (state == kTracing && ng.y > 0x00FFFFFFu) {
+            uint32_t bit = 31u - __clz(ng.y);
+            ng.y &= ~(1u << bit);
+            uint32_t slot = (bit - 24u) ^ r.oct;
+            uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
             if (ng.y > 0x00FFFFFFu) {
-                uint32_t bit = 31u - __clz(ng.y);
-                ng.y &= ~(1u << bit);
-                uint32_t slot = (bit - 24u) ^ r.oct;
-                uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
-                if (ng.y > 0x00FFFFFFu) {
-                    if (sp < kStack8) {
-                        stack[sp++] = ng;
-                    } else {
-                        raise_status(kErrBounds);
-                    }
-                }
-                uint32_t child_base, imask;
-                if (COUNT) ++c_nodes;
-                uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, tcur, child_base, tri_base, imask);
-                ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
-                tg = hitmask & 0x00FFFFFFu;
-            } else {
-                tri_base = ng.x;
-                tg = ng.y;
-                ng = make_uint2(0u, 0u);
-            }
-            if (postpone != 0u) {
-                uint32_t with_tris = __ballot_sync(busy, tg != 0u);
-                if (tg != 0u && ng.y > 0x00FFFFFFu && (uint32_t)__popc(with_tris) < postpone && sp < kStack8) {
-                    stack[sp++] = make_uint2(tri_base, tg);
-                    tg = 0;
+                if (sp < kStack8) {
+                    stack[sp++] = ng;
+                } else {
+                    raise_status(kErrBounds);
                 }
             }
+            uint32_t child_base, imask;
+            if (COUNT) ++c_nodes;
+            uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, tcur, child_base, tri_base, imask);
+            ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
+            tg = hitmask & 0x00FFFFFFu;
         }
+        if (state == kTracing && ng.y <= 0x00FFFFFFu && sp > 0) ng = stack[--sp];
 
-        // Warp-wide triangle list: exclusive scan of the per-lane counts.
+        // Append this step's pairs: exclusive scan of the per-lane counts.
         const uint32_t cnt = __popc(tg);
         uint32_t incl = cnt;
 #pragma unroll
@@ -686,17 +687,35 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
             if (lane >= (uint32_t)d) incl += v;
         }
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total != 0u) {
-            uint32_t pos = incl - cnt;
+        if (cnt != 0u) {
+            uint32_t pos = appended + incl - cnt;
             const uint32_t owner = lane << kRecBits;
             while (tg != 0u) {
                 uint32_t tb = __ffs(tg) - 1u;
                 tg &= tg - 1u;
-                task[pos++] = owner | (tri_base + tb);
+                task[pos++ & (kRing - 1)] = owner | (tri_base + tb);
             }
+            my_end = pos;
+            if (COUNT) c_tris += cnt;
+        }
+        appended += total;
+
+        // A tracing lane without nodes left waits for its own tests.
+        const bool waiting = state == kTracing && ng.y <= 0x00FFFFFFu;
+        const uint32_t walk_mask = __ballot_sync(0xffffffffu, state == kTracing && !waiting);
+        const uint32_t wait_mask = __ballot_sync(0xffffffffu, waiting && (int32_t)(my_end - tested) > 0);
+        const uint32_t pend = appended - tested;
+        uint32_t nflush = 0;
+        if (pend != 0u) {
+            if (walk_mask == 0u || batch <= 1u || (uint32_t)__popc(wait_mask | want_mask) >= refill)
+                nflush = pend;
+            else if (pend >= batch)
+                nflush = pend >= 32u ? (pend & ~31u) : pend;
+        }
+        if (nflush != 0u) {
             __syncwarp();
-            for (uint32_t j = lane; j < total; j += 32u) {
-                const uint32_t w = task[j];
+            for (uint32_t j = lane; j < nflush; j += 32u) {
+                const uint32_t w = task[(tested + j) & (kRing - 1)];
                 const uint32_t o = wbase + (w >> kRecBits);
                 const uint32_t rec = w & ((1u << kRecBits) - 1u);
                 const RayS rs = s_ray[o];
@@ -715,23 +734,19 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
                 }
             }
             __syncwarp();
-            if (COUNT) c_tris += cnt;
+            tested += nflush;
         }
 
         if (state == kTracing) {
             const unsigned long long best = s_best[threadIdx.x];
             tcur = hit_key_t(best);
-            bool finished = false;
+            bool stop = waiting;
             if (!CLOSEST && (uint32_t)best != 0xFFFFFFFFu) {
-                finished = true;
-            } else if (ng.y <= 0x00FFFFFFu) {
-                if (sp == 0) {
-                    finished = true;
-                } else {
-                    ng = stack[--sp];
-                }
+                stop = true;  // any hit: no more node steps
+                ng.y = 0u;
+                sp = 0;
             }
-            if (finished) {
+            if (stop && (int32_t)(my_end - tested) <= 0) {
                 state = kDone;
                 if (COUNT) ++c_rays;
             }
@@ -761,6 +776,9 @@ static uint32_t g_refill = 8;
 void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
 static uint32_t g_postpone = 0;
 void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
+static uint32_t g_batch = 24;
+void set_trace_batch(uint32_t pairs) { g_batch = pairs < 1 ? 1 : (pairs > 32 ? 32 : pairs); }
+uint32_t get_trace_batch() { return g_batch; }
 static bool g_coop = true;
 void set_trace_coop(bool on) { g_coop = on; }
 bool get_trace_coop() { return g_coop; }
@@ -828,7 +846,7 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
                               : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);
             k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, sc.bvh8_rec_of_key,
-                                        work, g_refill, g_postpone);
+                                        work, g_refill, g_batch);
         } else {
             auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
                               : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);
