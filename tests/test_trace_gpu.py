@@ -173,17 +173,17 @@ def test_multi_geometry_ids(wf, dev):
     assert np.all(hit[hit[:, 1] == 1, 0] < 1500) and np.all(hit[hit[:, 1] == 2, 0] < 500)
 
 
-@pytest.mark.parametrize("coop,batch", [(0, 24), (1, 1), (1, 7), (1, 24), (1, 32)])
+@pytest.mark.parametrize("coop,batch,steps", [(0, 16, 2), (1, 1, 1), (1, 7, 1), (1, 16, 2), (1, 32, 3), (1, 24, 8)])
 @pytest.mark.parametrize("refill,postpone", [(1, 0), (32, 0), (8, 8), (4, 16)])
-def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone, coop, batch):
+def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone, coop, batch, steps):
     pos, idx, sc = soup
     rays = random_rays(np.random.default_rng(12), 60000)
     ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
     ref_any = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=False)
-    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch")
+    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch", "trace.bvh8.steps")
     old = [wf.api.tune_get(k) for k in keys]
     try:
-        for k, v in zip(keys, (refill, postpone, coop, batch)):
+        for k, v in zip(keys, (refill, postpone, coop, batch, steps)):
             wf.api.tune_set(k, v)
         assert np.array_equal(gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays), ref)
         a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)

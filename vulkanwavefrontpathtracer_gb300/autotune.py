@@ -37,30 +37,34 @@ def _timeit(fn: Callable[[], None], reps: int = 5, warm: int = 2) -> float:
 
 def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[int] = (1, 2, 4, 8, 16, 32),
                    postpones: Iterable[int] = (0, 4, 8, 12), coops: Iterable[int] = (0, 1),
-                   batches: Iterable[int] = (1, 8, 16, 24, 32), reps: int = 5) -> Dict:
-    """Grid search of refill x (cooperative tests: batch; per-lane tests:
-    postpone) for BVH8 closest-hit and any-hit traversal; returns the best
-    settings and the full table (ms)."""
+                   batches: Iterable[int] = (1, 8, 16, 24, 32), steps: Iterable[int] = (1, 2, 3),
+                   reps: int = 5) -> Dict:
+    """Grid search of refill x (cooperative tests: batch x node steps per
+    iteration; per-lane tests: postpone) for BVH8 closest-hit and any-hit
+    traversal; returns the best settings and the full table (ms)."""
     import torch
     dev = closest_rays.device
     res_c = torch.empty((closest_rays.shape[0], 4), dtype=torch.int32, device=dev)
     res_a = torch.empty((any_rays.shape[0], 4), dtype=torch.int32, device=dev)
-    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch")
+    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch", "trace.bvh8.steps")
     old = [api.tune_get(k) for k in keys]
     grid = []
     for coop in coops:
         for refill in refills:
-            for v in (batches if coop else postpones):
-                grid.append((refill, 0 if coop else v, coop, v if coop else old[3]))
+            if coop:
+                grid += [(refill, 0, 1, b, s) for b, s in itertools.product(batches, steps)]
+            else:
+                grid += [(refill, p, 0, old[3], old[4]) for p in postpones]
     table = []
     try:
-        for refill, post, coop, batch in grid:
-            for k, v in zip(keys, (refill, post, coop, batch)):
+        for setting in grid:
+            for k, v in zip(keys, setting):
                 api.tune_set(k, v)
             mc = _timeit(lambda: api.trace(scene, L.BVH8_Q8, closest_rays, res_c, closest_hit=True), reps)
             ma = _timeit(lambda: api.trace(scene, L.BVH8_Q8, any_rays, res_a, closest_hit=False), reps)
-            table.append({"refill": refill, "postpone": post, "coop": coop, "batch": batch, "closest_ms": mc,
-                          "any_ms": ma})
+            refill, post, coop, batch, stp = setting
+            table.append({"refill": refill, "postpone": post, "coop": coop, "batch": batch, "steps": stp,
+                          "closest_ms": mc, "any_ms": ma})
     finally:
         for k, v in zip(keys, old):
             api.tune_set(k, v)
@@ -68,7 +72,7 @@ def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[i
     nc, na = closest_rays.shape[0], any_rays.shape[0]
     best = min(table, key=lambda e: e["closest_ms"] + e["any_ms"])
     return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "batch": best["batch"],
-            "table": table, "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
+            "steps": best["steps"], "table": table, "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
             "best_any_mrays_s": na / (best["any_ms"] * 1e-3) / 1e6}
 
 
@@ -228,3 +232,5 @@ def apply(traversal: Dict) -> None:
         api.tune_set("trace.bvh8.coop", traversal["coop"])
     if "batch" in traversal:
         api.tune_set("trace.bvh8.batch", traversal["batch"])
+    if "steps" in traversal:
+        api.tune_set("trace.bvh8.steps", traversal["steps"])

@@ -104,6 +104,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_trace_batch((uint32_t)value);
         return WFPT_OK;
     }
+    if (k == "trace.bvh8.steps") {
+        if (value < 1 || value > 8) return invalid("trace.bvh8.steps must be in [1, 8]");
+        wfpt::set_trace_steps((uint32_t)value);
+        return WFPT_OK;
+    }
     if (k == "trace.bvh8.coop") {
         if (value < 0 || value > 1) return invalid("trace.bvh8.coop must be 0 or 1");
         wfpt::set_trace_coop(value != 0);
@@ -168,6 +173,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "trace.bvh8.batch") {
         *value = (int64_t)wfpt::get_trace_batch();
+        return WFPT_OK;
+    }
+    if (k == "trace.bvh8.steps") {
+        *value = (int64_t)wfpt::get_trace_steps();
         return WFPT_OK;
     }
     if (k == "trace.bvh8.coop") {

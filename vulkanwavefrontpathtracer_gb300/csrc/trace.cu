@@ -582,19 +582,23 @@ constexpr int kRing = 1024;        // per-warp ring of pending triangle tests (p
 // Tests are batched across node steps: the ring is tested once `batch` or
 // more pairs are pending (in whole passes of 32 when 32 or more are), and
 // entirely once the lanes waiting on their own tests plus the idle lanes
-// would fill a refill, or no lane has nodes left.  A lane's ray finishes
+// would fill a refill, or no lane has nodes left.  A loop iteration takes up
+// to `steps` node steps per lane, stopping at the first node that hands the
+// lane triangles, so the per-iteration work (refill check, votes, scan,
+// test decision) is shared by several node steps.  A lane's ray finishes
 // only when its traversal is exhausted (any hit: when it has a hit) and all
 // of its own tests have run, so a ring entry never outlives its ray.  The
 // deferred tests leave tcur larger for a few node steps (culling stays
 // conservative: tcur only shrinks), which costs about 1 % more node steps
 // and saves most of the partly empty test passes (batch 1: test every
-// step).  At most 31 + 32 * 24 pairs are pending after an append.
+// step).  A lane appends at most one node's 24 triangles per iteration, so
+// at most 31 + 32 * 24 pairs are pending after an append.
 template <bool CLOSEST, bool COUNT>
 __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
     const float4* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
     int4* __restrict__ results, const uint32_t* __restrict__ ray_index, uint32_t n,
     const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ rec_of_key, uint32_t* __restrict__ work,
-    uint32_t refill, uint32_t batch) {
+    uint32_t refill, uint32_t batch, uint32_t steps) {
     __shared__ RayS s_ray[kBlock];
     __shared__ unsigned long long s_best[kBlock];
     __shared__ uint32_t s_task[kBlock / 32][kRing];
@@ -657,26 +661,32 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
         if (__ballot_sync(0xffffffffu, state != kIdle || !exhausted) == 0u) break;
         if (COUNT && lane == 0) ++c_iters;
 
+        // Up to `steps` node steps; a lane stops stepping at the first node
+        // that hands it triangles (at most one group of 24 per iteration).
         uint32_t tri_base = 0, tg = 0;
-        if (state == kTracing && ng.y > 0x00FFFFFFu) {
-            uint32_t bit = 31u - __clz(ng.y);
-            ng.y &= ~(1u << bit);
-            uint32_t slot = (bit - 24u) ^ r.oct;
-            uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
-            if (ng.y > 0x00FFFFFFu) {
-                if (sp < kStack8) {
-                    stack[sp++] = ng;
-                } else {
-                    raise_status(kErrBounds);
+        for (uint32_t st = 0; st < steps; ++st) {
+            const bool go = state == kTracing && ng.y > 0x00FFFFFFu && tg == 0u;
+            if (st != 0u && !__any_sync(0xffffffffu, go)) break;
+            if (go) {
+                uint32_t bit = 31u - __clz(ng.y);
+                ng.y &= ~(1u << bit);
+                uint32_t slot = (bit - 24u) ^ r.oct;
+                uint32_t node = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+                if (ng.y > 0x00FFFFFFu) {
+                    if (sp < kStack8) {
+                        stack[sp++] = ng;
+                    } else {
+                        raise_status(kErrBounds);
+                    }
                 }
+                uint32_t child_base, imask;
+                if (COUNT) ++c_nodes;
+                uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, tcur, child_base, tri_base, imask);
+                ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
+                tg = hitmask & 0x00FFFFFFu;
             }
-            uint32_t child_base, imask;
-            if (COUNT) ++c_nodes;
-            uint32_t hitmask = intersect_node8(nodes + 5 * (size_t)node, r, tcur, child_base, tri_base, imask);
-            ng = make_uint2(child_base, (hitmask & 0xFF000000u) | imask);
-            tg = hitmask & 0x00FFFFFFu;
+            if (state == kTracing && ng.y <= 0x00FFFFFFu && sp > 0) ng = stack[--sp];
         }
-        if (state == kTracing && ng.y <= 0x00FFFFFFu && sp > 0) ng = stack[--sp];
 
         // Append this step's pairs: exclusive scan of the per-lane counts.
         const uint32_t cnt = __popc(tg);
@@ -776,7 +786,10 @@ static uint32_t g_refill = 8;
 void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
 static uint32_t g_postpone = 0;
 void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
-static uint32_t g_batch = 24;
+static uint32_t g_batch = 16;
+static uint32_t g_steps = 2;
+void set_trace_steps(uint32_t steps) { g_steps = steps < 1 ? 1 : (steps > 8 ? 8 : steps); }
+uint32_t get_trace_steps() { return g_steps; }
 void set_trace_batch(uint32_t pairs) { g_batch = pairs < 1 ? 1 : (pairs > 32 ? 32 : pairs); }
 uint32_t get_trace_batch() { return g_batch; }
 static bool g_coop = true;
@@ -846,7 +859,7 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
                               : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);
             k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, sc.bvh8_rec_of_key,
-                                        work, g_refill, g_batch);
+                                        work, g_refill, g_batch, g_steps);
         } else {
             auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
                               : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);

@@ -17,6 +17,8 @@ void set_trace_refill(uint32_t refill);
 void set_trace_postpone(uint32_t lanes);
 void set_trace_batch(uint32_t pairs);
 uint32_t get_trace_batch();
+void set_trace_steps(uint32_t steps);
+uint32_t get_trace_steps();
 uint32_t get_trace_refill();
 uint32_t get_trace_postpone();
 // Warp-cooperative triangle tests in the BVH8 traversal (on by default).
