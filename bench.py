@@ -137,10 +137,74 @@ def setup_dist():
 
 
 # ------------------------------------------------------------------ ours
-def city_bounce(wf, api, dev, stream):
+def city_frames(wf, api, dev, stream, scene, geom, steps=3):
+    """Whole city frames (3840x2160, 1 spp, 8 bounces, 2 shadow samples):
+    the chosen form as specified (BVH8, sort + reorder of every bounce,
+    graph replay, overlapped shadow passes), the plain form, and the chosen
+    form as autotuned on this GPU (per-bounce reordering, then the BVH of the
+    bounces and of the primary pass, searched on whole frames).  Mrays/s
+    over all rays of a frame, CUDA events on the launching stream."""
+    import torch
+
+    from vulkanwavefrontpathtracer_gb300 import autotune
+    W = CITY
+    w, h = W["width"], W["height"]
+    cam = api.make_camera(**W["camera"])
+    rcfg = dict(COURTYARD["renderer"], **W["renderer"])
+    px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+
+    def make(form):
+        r = api.Renderer(**rcfg, **form)
+        r.set_scene(scene, geom, W["light"], W["background"])
+        return r
+
+    def timed(form, warm=1):
+        r = make(form)
+        for _ in range(warm):
+            r.render(cam, w, h, px, fp)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            r.render(cam, w, h, px, fp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        st = r.stats()
+        r.close()
+        ms = a.elapsed_time(b) / steps
+        rays = st.num_primary_rays + st.num_shadow_rays + st.num_path_rays
+        return ms, rays
+
+    c_ms, rays = timed(CHOSEN)
+    p_ms, _ = timed(PLAIN)
+    depth = rcfg["recursion_depth"]
+    tune = autotune.tune_bounce_sort(lambda m: make(dict(CHOSEN, path_sort_skip=m)), cam, w, h, depth, frames=2,
+                                     device=dev)
+    mask = int(tune["path_sort_skip"])
+    ktune = autotune.tune_bvh_kinds(
+        lambda k, pk: make(dict(CHOSEN, path_sort_skip=mask, bvh_kind=k, primary_bvh_kind=pk)), cam, w, h, frames=2,
+        device=dev)
+    kinds = dict(bvh_kind=int(ktune["bvh_kind"]), primary_bvh_kind=int(ktune["primary_bvh_kind"]))
+    t_ms, _ = timed(dict(CHOSEN, path_sort_skip=mask, **kinds))
+    mr = lambda ms: round(rays / (ms * 1e-3) / 1e6, 3)
+    return {"resolution": [w, h], "rays_per_frame": int(rays),
+            "chosen": {"value": mr(c_ms), "unit": "Mrays/s", "ms_per_frame": round(c_ms, 3)},
+            "plain": {"value": mr(p_ms), "unit": "Mrays/s", "ms_per_frame": round(p_ms, 3)},
+            "chosen_over_plain": round(p_ms / c_ms, 3),
+            "autotuned": {"value": mr(t_ms), "unit": "Mrays/s", "ms_per_frame": round(t_ms, 3),
+                          "over_plain": round(p_ms / t_ms, 3), "path_sort_skip": mask, **kinds,
+                          "search": [{"path_sort_skip": e["path_sort_skip"], "ms": round(e["ms"], 3)}
+                                     for e in tune["table"]]
+                          + [{"bvh_kind": e["bvh_kind"], "primary_bvh_kind": e["primary_bvh_kind"],
+                              "ms": round(e["ms"], 3)} for e in ktune["table"]]}}
+
+
+def city_bounce(wf, api, dev, stream, frames=True):
     """The bounce-1 comparison of `bounce_micro` on the city block at
-    3840x2160 (8.3M primary rays).  Returns its per-bounce line and the
-    host-built city scene (for the build-time report)."""
+    3840x2160 (8.3M primary rays) and, with `frames`, whole city frames
+    (city_frames).  Returns the per-bounce line (with the frames under
+    "frames") and the host-built city scene (for the build-time report)."""
     W = CITY
     pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
     scene = api.Scene(pos, idx)
@@ -151,6 +215,9 @@ def city_bounce(wf, api, dev, stream):
     line["triangles"] = int(scene.info.num_triangles)
     line["resolution"] = [W["width"], W["height"]]
     line["sort_gbs"] = round(micro["sort"]["gbs"], 1)
+    del micro
+    if frames:
+        line["frames"] = city_frames(wf, api, dev, stream, scene, geom)
     del geom
     return line, (pos, idx, scene)
 
@@ -255,10 +322,11 @@ def run_ours(args):
     tune = autotune.tune_bounce_sort(lambda m: make(dict(CHOSEN, path_sort_skip=m)), cam, w, h,
                                      W["renderer"]["recursion_depth"], frames=3, device=dev)
     mask = int(tune["path_sort_skip"])
-    ptune = autotune.tune_primary_bvh(lambda k: make(dict(CHOSEN, path_sort_skip=mask, primary_bvh_kind=k)), cam, w,
-                                      h, frames=3, device=dev)
-    pkind = int(ptune["primary_bvh_kind"])
-    tuned = make(dict(CHOSEN, path_sort_skip=mask, primary_bvh_kind=pkind))
+    ktune = autotune.tune_bvh_kinds(
+        lambda k, pk: make(dict(CHOSEN, path_sort_skip=mask, bvh_kind=k, primary_bvh_kind=pk)), cam, w, h, frames=3,
+        device=dev)
+    bkind, pkind = int(ktune["bvh_kind"]), int(ktune["primary_bvh_kind"])
+    tuned = make(dict(CHOSEN, path_sort_skip=mask, bvh_kind=bkind, primary_bvh_kind=pkind))
     ms_t, rays_t, _, _ = timed_frames(tuned, args.steps, max(1, args.warmup // 2))
     tuned_value = rays_t / (ms_t * 1e-3) / 1e6
 
@@ -322,15 +390,15 @@ def run_ours(args):
             "chosen_over_plain": round(value / plain_value, 3),
             "autotuned": {"value": round(tuned_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_t / args.steps, 4),
                           "over_plain": round(tuned_value / plain_value, 3), "path_sort_skip": mask,
-                          "primary_bvh_kind": pkind,
+                          "bvh_kind": bkind, "primary_bvh_kind": pkind,
                           "search": [{"path_sort_skip": e["path_sort_skip"], "ms": round(e["ms"], 3)}
                                      for e in tune["table"]]
-                          + [{"primary_bvh_kind": e["primary_bvh_kind"], "ms": round(e["ms"], 3)}
-                             for e in ptune["table"]],
+                          + [{"bvh_kind": e["bvh_kind"], "primary_bvh_kind": e["primary_bvh_kind"],
+                              "ms": round(e["ms"], 3)} for e in ktune["table"]],
                           "note": "chosen form with the per-bounce reordering (autotune.tune_bounce_sort; bit b "
-                                  "set: bounce b+1 unsorted) and the primary pass's BVH (tune_primary_bvh; 0 = "
-                                  "FP32 BVH2 for the coherent camera rays) picked live; incoherent bounces use "
-                                  "the BVH8"},
+                                  "set: bounce b+1 unsorted) and the BVH of the bounces and of the primary pass "
+                                  "(autotune.tune_bvh_kinds; 0 = FP32 BVH2, 1 = BVH8, -1 = as the bounces) "
+                                  "picked live on whole frames"},
             "per_bounce": micro["per_bounce"],
             "per_bounce_city": city_line,
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
@@ -531,7 +599,7 @@ def run_micro_only(args):
     dev = torch.device("cuda", 0)
     api = wf.api
     if args.city:
-        line, _ = city_bounce(wf, api, dev, torch.cuda.current_stream())
+        line, _ = city_bounce(wf, api, dev, torch.cuda.current_stream(), frames=not args.no_city_frames)
         print(json.dumps({"per_bounce_city": line}))
         return
     W = COURTYARD
@@ -855,7 +923,8 @@ def main():
     ap.add_argument("--micro-only", action="store_true",
                     help="only the bounce-1 microbenchmark (small profiling case with --width/--height)")
     ap.add_argument("--city", action="store_true",
-                    help="with --micro-only: the bounce-1 comparison on the city block at 3840x2160")
+                    help="with --micro-only: the bounce-1 comparison and whole frames on the city block at 3840x2160")
+    ap.add_argument("--no-city-frames", action="store_true", help="with --city: the bounce-1 comparison only")
     ap.add_argument("--width", type=int, default=COURTYARD["width"])
     ap.add_argument("--height", type=int, default=COURTYARD["height"])
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")

@@ -204,6 +204,33 @@ def tune_primary_bvh(make_renderer, camera, width: int, height: int, frames: int
     return {"primary_bvh_kind": best["primary_bvh_kind"], "ms": best["ms"], "table": table}
 
 
+def tune_bvh_kinds(make_renderer, camera, width: int, height: int, frames: int = 3, device=None) -> Dict:
+    """BVH of the bounces and of the primary pass: make_renderer(bvh_kind,
+    primary_bvh_kind) returns a renderer with its scene set; whole frames are
+    timed with the BVH8 everywhere, the FP32 BVH2 for the primary pass only,
+    and the FP32 BVH2 everywhere.  Returns the fastest pair and the table
+    (median ms of `frames` frames)."""
+    import statistics
+
+    import torch
+    dev = device or torch.device("cuda", 0)
+    px = torch.zeros((width * height, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+    table = []
+    for kind, pkind in ((L.BVH8_Q8, -1), (L.BVH8_Q8, L.BVH2_FP32), (L.BVH2_FP32, -1)):
+        r = make_renderer(kind, pkind)
+        r.render(camera, width, height, px, fp)
+        times = []
+        for _ in range(frames):
+            r.render(camera, width, height, px, fp)
+            times.append(r.stats().frame_ms)
+        r.close()
+        table.append({"bvh_kind": kind, "primary_bvh_kind": pkind, "ms": statistics.median(times)})
+    best = min(table, key=lambda e: e["ms"])
+    return {"bvh_kind": best["bvh_kind"], "primary_bvh_kind": best["primary_bvh_kind"], "ms": best["ms"],
+            "table": table}
+
+
 def measure_work(scene: api.Scene, rays, bvh_kind: int, closest: bool) -> Dict:
     """Node visits and triangle tests per ray (counting kernel variants)."""
     import torch
