@@ -136,6 +136,23 @@ def setup_dist():
     return world, rank, local
 
 
+def reduce_over_ranks(ms, rays, world, device):
+    """Job-wide result of one timed region: the slowest rank's time and the
+    rays all ranks traced.  The ranks meet at a barrier first, so none
+    leaves the timed region's accounting early; world == 1 returns the
+    inputs.  Replicas share nothing else: no collective touches the data
+    path."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    rt = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(rt, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(rt.item())
+
+
 # ------------------------------------------------------------------ ours
 def city_frames(wf, api, dev, stream, scene, geom, steps=3):
     """Whole city frames (3840x2160, 1 spp, 8 bounces, 2 shadow samples):
@@ -299,13 +316,8 @@ def run_ours(args):
         launches = lib.wfpt_kernel_launch_count() - l0
         st = r.stats()
         rays = (st.num_primary_rays + st.num_shadow_rays + st.num_path_rays) * steps
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        rt = torch.tensor([float(rays)], dtype=torch.float64, device=dev)
-        if world > 1:
-            dist.barrier()
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dist.all_reduce(rt, op=dist.ReduceOp.SUM)
-        return float(t.item()), float(rt.item()), st, launches
+        ms, rays = reduce_over_ranks(ms, rays, world, dev)
+        return ms, rays, st, launches
 
     # Headline: the courtyard configuration as specified, every bounce's
     # path rays Morton-sorted and reordered.  Beside it, the per-bounce
@@ -337,6 +349,9 @@ def run_ours(args):
         chosen.render(cam, w, h, px, fp)
         host_img.copy_(fp, non_blocking=True)
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
@@ -344,9 +359,9 @@ def run_ours(args):
         host_img.copy_(fp, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
     rays_per_frame = st_c.num_primary_rays + st_c.num_shadow_rays + st_c.num_path_rays
-    e2e_value = rays_per_frame * args.steps / (e2e_ms * 1e-3) / 1e6 * world
+    e2e_ms, e2e_rays = reduce_over_ranks(e0.elapsed_time(e1), rays_per_frame * args.steps, world, dev)
+    e2e_value = e2e_rays / (e2e_ms * 1e-3) / 1e6
 
     micro = bounce_micro(wf, api, dev, scene, geom, cam, w, h, stream)
     hbm, peak_kind = peaks()
