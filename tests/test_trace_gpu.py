@@ -142,6 +142,43 @@ def test_miss_record_and_device_count(wf, dev, soup):
     assert np.all(o[600:] == 5)
 
 
+@pytest.mark.parametrize("batch,steps", [(1, 1), (16, 2), (32, 3)])
+@pytest.mark.parametrize("closest", [True, False])
+def test_bvh8_batched_tests_indirect_device_count(wf, dev, soup, batch, steps, closest):
+    """Batched cooperative tests with an indirect index, empty intervals and
+    a device-side count below n: the first count rays (through the index)
+    get the BVH2's hit (any hit: its hit flag), the rest are untouched."""
+    import torch
+    pos, idx, sc = soup
+    rng = np.random.default_rng(31 + batch + steps)
+    n, count = 40000, 27777
+    rays = random_rays(rng, n)
+    rays[::7, 7] = -1.0  # tmax < tmin: miss
+    perm = rng.permutation(n).astype(np.uint32)
+    ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=closest)
+    keys = ("trace.bvh8.batch", "trace.bvh8.steps")
+    old = [wf.api.tune_get(k) for k in keys]
+    try:
+        for k, v in zip(keys, (batch, steps)):
+            wf.api.tune_set(k, v)
+        out = torch.full((n, 4), 77, dtype=torch.int32, device=dev)
+        cnt = torch.tensor([count], dtype=torch.int32, device=dev)
+        wf.api.trace(sc, wf.BVH8_Q8, T(rays, dev), out, ray_index=T(perm.view(np.int32), dev), n_dev=cnt,
+                     closest_hit=closest)
+        o = N(out)
+    finally:
+        for k, v in zip(keys, old):
+            wf.api.tune_set(k, v)
+    done = perm[:count]
+    rest = np.setdiff1d(np.arange(n), done)
+    if closest:
+        assert np.array_equal(o[done], ref[done])
+    else:
+        assert np.array_equal(o[done, 0] >= 0, ref[done, 0] >= 0)
+    assert np.all(o[rest] == 77)
+    assert wf.api.device_status() == 0
+
+
 def test_empty_and_tiny_scenes(wf, dev):
     pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
     idx = np.array([[0, 1, 2]], np.uint32)
