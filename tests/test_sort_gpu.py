@@ -150,3 +150,37 @@ def test_sort_tile_variants(wf, dev, tiles, n, key_bits, digit_bits):
     rk, rv = stable_ref(keys, key_bits)
     assert np.array_equal(v, rv) and np.array_equal(k, rk)
     assert wf.api.device_status() == 0
+
+
+@pytest.mark.parametrize("key_bits", [63, 32])
+def test_sort_full_size_properties(wf, dev, key_bits):
+    """2^26 pairs, the microbenchmark's largest size (beyond what a CPU
+    stable sort checks quickly): keys non-decreasing, values a permutation,
+    each output key the input key its value points at, and equal keys in
+    input order (values are the input positions, so they increase within
+    a run of equal keys).  Keys are drawn from a quarter of n values, so
+    most keys repeat."""
+    import torch
+    n = 1 << 26
+    g = torch.Generator(device=dev)
+    g.manual_seed(key_bits)
+    hi = (1 << 62) if key_bits > 32 else (1 << 31)
+    pool = torch.randint(0, hi, (n // 4,), generator=g, device=dev, dtype=torch.int64)
+    src = pool[torch.randint(0, n // 4, (n,), generator=g, device=dev)]
+    if key_bits <= 32:
+        src = src.to(torch.int32)
+    keys = src.clone()
+    vals = torch.arange(n, dtype=torch.int32, device=dev)
+    wf.api.sort_pairs(keys, vals, key_bits)
+    torch.cuda.synchronize()
+    assert wf.api.device_status() == 0
+    k = keys.to(torch.int64)
+    if key_bits <= 32:
+        k = k & 0xFFFFFFFF  # compare as unsigned 32-bit
+    assert bool((k[1:] >= k[:-1]).all())
+    v = vals.to(torch.int64)
+    assert bool((torch.bincount(v, minlength=n) == 1).all())
+    assert bool((keys == src[v]).all())
+    same = k[1:] == k[:-1]
+    assert bool((v[1:][same] > v[:-1][same]).all())
+    assert int(same.sum()) > n // 2

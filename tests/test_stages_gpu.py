@@ -276,3 +276,26 @@ def test_fill(wf, dev):
     t = torch.zeros(1000003, dtype=torch.float32, device=dev)
     wf.api.fill_u32(t, int(np.float32(1.0).view(np.uint32)), t.numel())
     assert bool((t == 1.0).all())
+
+
+def test_reorder_full_size_properties(wf, dev):
+    """The reorder gather at the city's 8,294,400 rays: out[i] = in[idx[i]],
+    the slot map follows the rays and index_to_slot inverts it."""
+    import torch
+    n = 3840 * 2160
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    rays = torch.rand((n, 8), generator=g, device=dev)
+    idx = torch.randperm(n, generator=g, device=dev).to(torch.int32)
+    s2i = torch.randperm(n, generator=g, device=dev).to(torch.int32)
+    out = torch.empty_like(rays)
+    os2i = torch.empty(n, dtype=torch.int32, device=dev)
+    oi2s = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    wf.api.reorder(idx, rays, out, s2i, os2i, oi2s)
+    torch.cuda.synchronize()
+    assert wf.api.device_status() == 0
+    li = idx.to(torch.int64)
+    assert torch.equal(out, rays[li])
+    assert torch.equal(os2i, s2i[li])
+    slots = torch.arange(n, dtype=torch.int32, device=dev)
+    assert torch.equal(oi2s[os2i.to(torch.int64)], slots)
