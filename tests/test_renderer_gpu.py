@@ -189,3 +189,47 @@ def test_renderer_rejects_missing_bvh_kind(wf, dev):
     with pytest.raises(wf.WfptError):
         r2.render(wf.api.make_camera(**CAM), 16, 16, px, px.clone())
     assert wf.api.device_status() == 0
+
+
+@pytest.mark.parametrize("workload", ["COURTYARD", "CITY"])
+def test_full_size_frames_identical_across_forms(wf, dev, workload):
+    """Whole frames at the benchmark's sizes (courtyard 1920x1080, city
+    block 3840x2160, 8 bounces, sorted path rays): BVH8 or FP32 BVH2 for the
+    bounces and the camera rays, graph replay or direct launches, shadow
+    passes overlapped or not -- the same pixels bit for bit (the CPU oracle
+    frame is checked at small sizes above; here the forms check each
+    other at full size)."""
+    import sys
+    from pathlib import Path
+
+    import torch
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+    W = getattr(bench, workload)
+    pos, nrm, idx = wf.api.generate_scene(W["scene_kind"], W["seed"])
+    sc = wf.api.Scene(pos, idx)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    cam = wf.api.make_camera(**W["camera"])
+    w, h = W["width"], W["height"]
+    rcfg = dict(bench.COURTYARD["renderer"], **W["renderer"])
+
+    def frame(**form):
+        r = wf.api.Renderer(**dict(rcfg, morton_kind=2, sort_path_rays=1, reorder_path_rays=1, **form))
+        r.set_scene(sc, geom, W["light"], W["background"])
+        px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+        fp = torch.zeros_like(px)
+        r.render(cam, w, h, px, fp)
+        st = r.stats()
+        out = _canon_nan(N(fp)).view(np.uint32)
+        r.close()
+        return out, (st.num_primary_rays, st.num_shadow_rays, st.num_path_rays)
+
+    ref, counts = frame(bvh_kind=wf.BVH8_Q8, use_graph=1, shadow_overlap=1)
+    assert counts[2] > 0
+    for form in (dict(bvh_kind=wf.BVH2_FP32, use_graph=0, shadow_overlap=0),
+                 dict(bvh_kind=wf.BVH8_Q8, primary_bvh_kind=wf.BVH2_FP32, use_graph=1, shadow_overlap=1),
+                 dict(bvh_kind=wf.BVH8_Q8, use_graph=0, shadow_overlap=0)):
+        got, c = frame(**form)
+        assert c == counts
+        assert np.array_equal(got, ref)
+    assert wf.api.device_status() == 0
