@@ -383,8 +383,7 @@ def run_ours(args):
                     "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_ray": 48,
                     "launch_ms": tr["ms"], "rays_per_launch": tr["rays"],
                     "note": "the BVH and triangles stay in L2, so DRAM carries only the ray and hit records; "
-                            "the kernel is bound by instruction issue (ncu: 74-76 % issue active, DRAM "
-                            "throughput 1.3-1.6 %; profiles/k_trace_bvh8_coop_courtyard_bounce1_960x540.md)"}
+                            "the kernel is bound by instruction issue, not by HBM"}
 
         roof = trace_roof(micro["trace_shadow"], "k_trace_bvh8_coop<any-hit> (bounce-1 shadow rays, 2 per path ray)",
                           "any")

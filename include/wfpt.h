@@ -301,8 +301,13 @@ wfpt_status wfpt_raygen_path(uint32_t* seeds, const wfpt_geometry* geometries,
  *   the call clears them itself, stream-ordered on `stream`, before its
  *   kernel.  The caller clears nothing.  *out_count_dev is written, not
  *   accumulated.
- * - The first call on each device looks up the array's device address with
- *   that device current; make that first call outside any stream capture.
+ * - The first call in each CUDA context (each device's primary context,
+ *   and again after cudaDeviceReset) looks up the array's device address
+ *   with cudaGetSymbolAddress; make that first call outside any stream
+ *   capture.  A first call made while `stream` is capturing launches
+ *   nothing and returns WFPT_ERR_INVALID_ARGUMENT with a message saying so.
+ *   The address is cached per context (by its unique id), so a later
+ *   context on the same device never uses a stale address.
  * - All calls on one device share the one array: calls that overlap in time
  *   (two streams with no event ordering them, or two host threads) race on
  *   it and give wrong output or WFPT_ERR_TIMEOUT from wfpt_device_status.

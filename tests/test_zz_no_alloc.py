@@ -1,8 +1,14 @@
 """wfpt_raygen_path_static (compaction over the library's fixed device
 scratch, no allocation) against wfpt_raygen_path with caller scratch, through
-the C ABI, on two calls in a row.  Collected last so that it also runs after
-every other GPU test in one process; it passes alone as well."""
+the C ABI, on two calls in a row, at n = 0 and at the array's maximum n.
+Collected last so that it also runs after every other GPU test in one
+process; it passes alone as well."""
 import ctypes as C
+import os
+import subprocess
+import sys
+import textwrap
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -84,3 +90,106 @@ def test_static_scratch_rejects_oversized_n(wf):
     n = wf.api.RAYGEN_PATH_STATIC_MAX_RAYS + 1
     assert lib.wfpt_raygen_path_static(buf, buf, buf, buf, buf, buf, buf, buf, buf, n, None, 0, 0.8, None) == 1
     assert b"WFPT_RAYGEN_PATH_STATIC_MAX_RAYS" in lib.wfpt_last_error_message()
+
+
+def _synthetic_inputs(n, ntri, dev, seed):
+    """Device-made inputs for sizes the CPU oracle cannot trace quickly:
+    random rays, and hit records naming random triangles of the geometry
+    (about a third of them misses) with random t and packed barycentrics."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    rays = torch.rand((n, 8), generator=g, device=dev)
+    d = torch.randn((n, 3), generator=g, device=dev)
+    rays[:, 4:7] = d / d.norm(dim=1, keepdim=True)
+    prim = torch.randint(0, ntri, (n,), generator=g, device=dev, dtype=torch.int32)
+    miss = torch.rand(n, generator=g, device=dev) < 0.35
+    res = torch.zeros((n, 4), dtype=torch.int32, device=dev)
+    res[:, 0] = torch.where(miss, torch.full_like(prim, -1), prim)
+    res[:, 1] = torch.where(miss, torch.full_like(prim, -1), torch.zeros_like(prim))
+    res[:, 2] = torch.where(miss, torch.full((n,), -1.0, device=dev),
+                            torch.rand(n, generator=g, device=dev) * 4 + 0.01).view(torch.int32)
+    u = torch.randint(0, 32768, (n,), generator=g, device=dev, dtype=torch.int32)
+    v = torch.randint(0, 32768, (n,), generator=g, device=dev, dtype=torch.int32)
+    res[:, 3] = u | (v << 16)
+    seeds = torch.randint(-2**31, 2**31 - 1, (n,), generator=g, device=dev, dtype=torch.int32)
+    i2p = torch.randperm(n, generator=g, device=dev).to(torch.int32)
+    dec = torch.rand((n, 4), generator=g, device=dev) * 0.9 + 0.1
+    return rays, res, seeds, i2p, dec
+
+
+def _run_dev(fn, geom, inp, n):
+    import torch
+    rays, res, seeds, i2p, dec = inp
+    d_seeds, d_dec = seeds.clone(), dec.clone()
+    out = torch.zeros((max(n, 1), 8), dtype=torch.float32, device=rays.device)
+    o_i2p = torch.zeros(max(n, 1), dtype=torch.int32, device=rays.device)
+    cnt = torch.full((1,), 777, dtype=torch.int32, device=rays.device)
+    fn(d_seeds, geom.table, rays, out, i2p, o_i2p, res, d_dec, cnt, n=n, albedo=0.8)
+    torch.cuda.synchronize()
+    c = int(cnt.item())
+    return c, out[:c], o_i2p[:c], d_seeds, d_dec
+
+
+def test_static_scratch_top_of_array_and_empty(wf, dev, scene):
+    """n = WFPT_RAYGEN_PATH_STATIC_MAX_RAYS uses every tile state of the
+    array (the last word included); n = 0 launches one idle block and must
+    write a zero count.  Both are compared with the caller-scratch entry."""
+    import torch
+    pos, nrm, idx, nodes, tris = scene
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    ntri = idx.reshape(-1, 3).shape[0]
+    n = wf.api.RAYGEN_PATH_STATIC_MAX_RAYS
+    inp = _synthetic_inputs(n, ntri, dev, 7)
+    ref = _run_dev(wf.api.raygen_path, geom, inp, n)
+    got = _run_dev(wf.api.raygen_path_static, geom, inp, n)
+    assert 0 < ref[0] < n
+    assert got[0] == ref[0]
+    for a, b in zip(got[1:], ref[1:]):
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    del inp, ref, got
+    empty = _synthetic_inputs(1, ntri, dev, 8)
+    for fn in (wf.api.raygen_path, wf.api.raygen_path_static):
+        assert _run_dev(fn, geom, empty, 0)[0] == 0
+    assert wf.api.device_status() == 0
+
+
+_CAPTURE_CHILD = textwrap.dedent("""
+    import sys
+    sys.path.insert(0, sys.argv[1])
+    import torch
+    import vulkanwavefrontpathtracer_gb300 as wf
+    lib = wf._lib.load()
+    dev = torch.device("cuda:0")
+    n = 1000
+    bufs = [torch.zeros(n * 8, dtype=torch.float32, device=dev) for _ in range(8)]
+    cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    args = [b.data_ptr() for b in bufs]
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        st = lib.wfpt_raygen_path_static(*args, cnt.data_ptr(), n, None, 0, 0.8, s.cuda_stream)
+    msg = lib.wfpt_last_error_message().decode()
+    assert st == 1, st
+    assert "capturing" in msg, msg
+    # Outside the capture the same call runs (every ray misses: zero hits).
+    res = torch.full((n, 4), -1, dtype=torch.int32, device=dev)
+    st = lib.wfpt_raygen_path_static(args[0], args[1], args[2], args[3], args[4], args[5], res.data_ptr(),
+                                     args[7], cnt.data_ptr(), n, None, 0, 0.8, None)
+    torch.cuda.synchronize()
+    assert st == 0, lib.wfpt_last_error_message()
+    assert int(cnt.item()) == 0
+    print("capture-check-ok")
+""")
+
+
+def test_static_scratch_first_call_under_capture_is_refused(wf):
+    """In a fresh process (a CUDA context where the entry point was never
+    called), a first call made while the stream is capturing launches nothing
+    and returns WFPT_ERR_INVALID_ARGUMENT; the next call outside the capture
+    works."""
+    root = str(Path(__file__).resolve().parents[1])
+    r = subprocess.run([sys.executable, "-c", _CAPTURE_CHILD, root], capture_output=True, text=True,
+                       timeout=300, env=dict(os.environ))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "capture-check-ok" in r.stdout

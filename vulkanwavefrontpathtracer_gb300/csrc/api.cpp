@@ -399,9 +399,13 @@ wfpt_status wfpt_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geomet
     WFPT_REQUIRE(n == 0 || (seeds && geometries && in_rays && out_rays && in_index_to_pixel && out_index_to_pixel &&
                             in_results && decreases),
                  "null buffer");
-    return from_cuda(wfpt::launch_raygen_path_static(seeds, geometries, in_rays, out_rays, in_index_to_pixel,
-                                                     out_index_to_pixel, in_results, decreases, out_count_dev, n,
-                                                     n_dev, albedo, S(stream)));
+    cudaError_t e = wfpt::launch_raygen_path_static(seeds, geometries, in_rays, out_rays, in_index_to_pixel,
+                                                    out_index_to_pixel, in_results, decreases, out_count_dev, n,
+                                                    n_dev, albedo, S(stream));
+    if (e == cudaErrorStreamCaptureUnsupported)
+        return invalid("first wfpt_raygen_path_static call in this CUDA context made while the stream is capturing; "
+                       "make one call outside any stream capture first (it looks up the scratch array's address)");
+    return from_cuda(e);
 }
 
 wfpt_status wfpt_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* results, const int32_t* index_to_pixel,

@@ -5,6 +5,9 @@
 // layouts and per-element semantics.  Launch shape: one thread per work
 // item, 256-thread blocks; every kernel honours an optional device-side
 // element count so that a frame can run without host readbacks.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <atomic>
 #include <mutex>
 
@@ -625,25 +628,73 @@ constexpr size_t kPathStaticWords = 1 + (WFPT_RAYGEN_PATH_STATIC_MAX_RAYS + kBlo
 static __device__ __align__(256) uint32_t g_path_static_scratch[kPathStaticWords];
 
 namespace {
-constexpr int kMaxDevices = 64;
+// Device addresses of g_path_static_scratch, one per CUDA context, keyed by
+// the context's unique id (cuCtxGetId: never reused within a process, so an
+// entry left by a context that was destroyed, for example by
+// cudaDeviceReset, can never match a later one).  The driver entry points
+// are resolved through the runtime, so the library does not link libcuda.
+struct StaticScratchEntry {
+    unsigned long long ctx_id;
+    uint32_t* ptr;
+};
+constexpr int kStaticScratchEntries = 64;
 std::mutex g_path_static_mu;
-uint32_t* g_path_static_ptr[kMaxDevices] = {};
+StaticScratchEntry g_path_static_cache[kStaticScratchEntries] = {};
+int g_path_static_next = 0;
+PFN_cuCtxGetCurrent_v4000 g_cu_ctx_get_current = nullptr;
+PFN_cuCtxGetId_v12000 g_cu_ctx_get_id = nullptr;
 
-// Device address of g_path_static_scratch on the current device, looked up
-// once per device (cudaGetSymbolAddress, with that device current).
-cudaError_t path_static_scratch(uint32_t** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+cudaError_t resolve_ctx_entry_points() {
+    if (g_cu_ctx_get_current && g_cu_ctx_get_id) return cudaSuccess;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+        return cudaErrorSymbolNotFound;
+    g_cu_ctx_get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f1);
+    g_cu_ctx_get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f2);
+    return cudaSuccess;
+}
+
+// Unique id of the context current on this thread; false when none is.
+bool current_ctx_id(unsigned long long* id) {
+    CUcontext ctx = nullptr;
+    if (g_cu_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return g_cu_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of g_path_static_scratch in the current context.  The
+// first call in a context looks it up with cudaGetSymbolAddress (which may
+// load the module); that first call is refused while `s` is capturing,
+// with cudaErrorStreamCaptureUnsupported, so that no lookup runs inside a
+// capture.  Later calls in the same context only read the cache.
+cudaError_t path_static_scratch(uint32_t** out, cudaStream_t s) {
     std::lock_guard<std::mutex> lock(g_path_static_mu);
-    if (!g_path_static_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_path_static_scratch);
-        if (e != cudaSuccess) return e;
-        g_path_static_ptr[dev] = static_cast<uint32_t*>(p);
+    cudaError_t e = resolve_ctx_entry_points();
+    if (e != cudaSuccess) return e;
+    unsigned long long id = 0;
+    if (current_ctx_id(&id)) {
+        for (const StaticScratchEntry& c : g_path_static_cache)
+            if (c.ptr && c.ctx_id == id) {
+                *out = c.ptr;
+                return cudaSuccess;
+            }
     }
-    *out = g_path_static_ptr[dev];
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) return e;
+    if (cap != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_path_static_scratch);
+    if (e != cudaSuccess) return e;
+    if (!current_ctx_id(&id)) return cudaErrorDeviceUninitialized;
+    g_path_static_cache[g_path_static_next] = StaticScratchEntry{id, static_cast<uint32_t*>(p)};
+    g_path_static_next = (g_path_static_next + 1) % kStaticScratchEntries;
+    *out = static_cast<uint32_t*>(p);
     return cudaSuccess;
 }
 }  // namespace
@@ -654,7 +705,7 @@ cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geom
                                       uint32_t n, const uint32_t* n_dev, float albedo, cudaStream_t s) {
     if (n > WFPT_RAYGEN_PATH_STATIC_MAX_RAYS) return cudaErrorInvalidValue;
     uint32_t* scratch = nullptr;
-    cudaError_t e = path_static_scratch(&scratch);
+    cudaError_t e = path_static_scratch(&scratch, s);
     if (e != cudaSuccess) return e;
     // The ticket and the tile states of this call's tiles start at zero.
     size_t tiles = ((size_t)n + kBlock - 1) / kBlock;
