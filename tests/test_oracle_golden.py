@@ -127,3 +127,30 @@ def test_shadow_ray_layout(orc):
     lens = np.linalg.norm(out[:3, 4:7], axis=1)
     assert np.allclose(lens, 1.0, atol=1e-6)
     assert np.all(out[3:, 7] == -1.0) and np.all(out[3:, 4] == 1.0) and np.all(out[3:, :3] == 0)
+
+
+def test_oracle_matches_reference_vectors(wf, orc):
+    """The oracle against outputs of the reference's own sources compiled for
+    the CPU (tests/golden/ref_vectors.npz), stage by stage."""
+    import refvectors as rv
+
+    def geom(pos, nrm, idx):
+        return orc.HostGeometry(wf.api.gltf_vertices(pos, nrm), idx)
+
+    impl = {
+        "init_seeds": orc.init_seeds,
+        "pixel_table": orc.pixel_table,
+        "camera": orc.camera_screen_to_world,
+        "raygen_primary": orc.raygen_primary,
+        "morton_aila32": lambda r, a, b: orc.morton(r, a, b, 0),
+        "reorder": orc.reorder,
+        "raygen_shadow": orc.raygen_shadow,
+        "raygen_path": lambda pos, nrm, idx, s, r, i2p, res, dec: orc.raygen_path(s, geom(pos, nrm, idx), r, i2p, res,
+                                                                                  dec, albedo=0.8),
+        "reconstruct_smooth": lambda pos, nrm, idx, r, res, i2p, px, dec, light, bg, spp: orc.reconstruct_smooth(
+            r, res, i2p, px, dec, geom(pos, nrm, idx), light, bg, spp),
+        "reconstruct_shadow": orc.reconstruct_shadow,
+        "count_hits": orc.count_hits,
+        "interpolate_colors": orc.interpolate_colors,
+    }
+    assert rv.check_all(impl) == rv.ALL_STAGES
