@@ -356,6 +356,18 @@ wfpt_status wfpt_interpolate_colors(float* frame_pixels, float* pixels,
                                     float key_value, float white_point,
                                     void* stream);
 
+/* interpolateColors.comp:71-98 with the running mean kept in double
+ * (the benchmark spec's FP64 per-pixel accumulation): accum holds one double4
+ * per pixel (xyz the mean, w unused; 32-byte aligned), written on every
+ * frame (frame 1: the frame's colour), blended on later frames with
+ * a = 1/frame, b = a * (frame - 1) in double; pixels receives the mean
+ * rounded to float (w as the float path writes it) and frame_pixels its
+ * Reinhard tone map. */
+wfpt_status wfpt_interpolate_colors_fp64(float* frame_pixels, float* pixels,
+                                         double* accum, uint32_t num_pixels,
+                                         int frame_index, float key_value,
+                                         float white_point, void* stream);
+
 /* vks::util::clearBuffer / clearBufferTimed with a 32-bit pattern
  * (Utils/BufferUtils.cpp; used by Renderer::initDecreases with 1.0f). */
 wfpt_status wfpt_fill_u32(void* dst, uint32_t pattern, size_t count_u32,
@@ -506,6 +518,24 @@ typedef struct wfpt_renderer_config {
                                        = bvh_kind, else a wfpt_bvh_kind.  On
                                        coherent camera rays the FP32 BVH2 is the
                                        faster one (the autotuner's choice). */
+    int timing;                     /* Application.mode "benchmark" with
+                                       Benchmark.printSortLogs: 0 (default) off;
+                                       1: the frame's stages are launched
+                                       directly on one stream (use_graph and
+                                       shadow_overlap are not applied) with CUDA
+                                       event pairs around them, which fill the
+                                       per-type trace times and the sort logs of
+                                       wfpt_render_stats; a sorted pass also
+                                       traces its rays unsorted first to log the
+                                       unsorted trace time, as the reference
+                                       does (Renderer.cpp:255-297).  Pixels and
+                                       ray counts are the same as without. */
+    int accumulate_fp64;            /* 0 (default): the running mean over frames
+                                       in float, as interpolateColors.comp; 1:
+                                       the mean kept in a double-precision
+                                       buffer of the renderer (32 bytes per
+                                       pixel), `pixels` gets its rounding to
+                                       float and the tone map reads that. */
 } wfpt_renderer_config;
 
 void wfpt_renderer_config_default(wfpt_renderer_config* config);
@@ -518,6 +548,18 @@ typedef struct wfpt_camera {
     float zfar;
 } wfpt_camera;
 
+/* SortLog (Renderer.h:29-46): one pass's ray count and the device times of
+ * its Morton keys, sort, reorder, sorted trace (traceSort's trace) and
+ * unsorted trace, in milliseconds, summed over the frame's primary samples. */
+typedef struct wfpt_sort_log {
+    uint64_t ray_count;
+    float morton_ms;
+    float sort_ms;
+    float reorder_ms;
+    float trace_sort_ms;
+    float trace_ms;
+} wfpt_sort_log;
+
 /* Statistics of the last frame (Renderer.cpp:660-714, Renderer.h:29-46). */
 typedef struct wfpt_render_stats {
     uint64_t num_primary_rays;
@@ -526,6 +568,19 @@ typedef struct wfpt_render_stats {
     uint32_t path_rays_per_bounce[8];
     uint32_t shadow_hits_per_pass[9];
     float frame_ms;                 /* device time of the whole frame */
+    /* With config.timing = 1 (else 0): getPrimaryTraceTime (raygenPrimary +
+     * trace), getShadowTraceTime (raygenShadow + trace or traceSort, every
+     * batch), getPathTraceTime (raygenPath + trace or traceSort), in ms;
+     * RT PERF of a ray type = its ray count * 1e-3 / its trace time. */
+    int timed;
+    float primary_trace_ms;
+    float shadow_trace_ms;
+    float path_trace_ms;
+    /* shadowSortLogs[0..depth] (0: the primary pass's shadow rays, b + 1:
+     * bounce b's) and pathSortLogs[0..depth-1]; times are filled for sorted
+     * passes, ray counts for every pass. */
+    wfpt_sort_log shadow_sort_logs[9];
+    wfpt_sort_log path_sort_logs[8];
 } wfpt_render_stats;
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config,

@@ -381,15 +381,42 @@ public:
         check(wfpt_renderer_get_stats(r_, &s));
         return s;
     }
-    /* Mrays/s of the last frame over all rays (primary + shadow + path). */
-    float getTracePerformance() {
+    /* Renderer::getNumberOf*Rays (Renderer.cpp:660-674) of the last frame. */
+    unsigned long long getNumberOfPrimaryRays() { return stats().num_primary_rays; }
+    unsigned long long getNumberOfShadowRays() { return stats().num_shadow_rays; }
+    unsigned long long getNumberOfPathRays() { return stats().num_path_rays; }
+    unsigned long long getNumberOfRays() {
         const wfpt_render_stats s = stats();
-        const double rays = (double)(s.num_primary_rays + s.num_shadow_rays + s.num_path_rays);
-        return s.frame_ms > 0.0f ? (float)(rays * 1e-3 / s.frame_ms) : 0.0f;
+        return s.num_primary_rays + s.num_shadow_rays + s.num_path_rays;
     }
+    /* Renderer::get*TraceTime (Renderer.cpp:676-690), in ms: filled when the
+     * config's timing option is on (the reference's benchmark mode), else 0. */
+    float getPrimaryTraceTime() { return stats().primary_trace_ms; }
+    float getShadowTraceTime() { return stats().shadow_trace_ms; }
+    float getPathTraceTime() { return stats().path_trace_ms; }
+    float getTraceTime() {
+        const wfpt_render_stats s = stats();
+        return s.primary_trace_ms + s.shadow_trace_ms + s.path_trace_ms;
+    }
+    /* Renderer::get*TracePerformance (Renderer.cpp:692-706): Mrays/s = rays *
+     * 1e-3 / trace ms, 0 when the trace time is 0 (timing off). */
+    float getPrimaryTracePerformance() { return perf(stats().num_primary_rays, getPrimaryTraceTime()); }
+    float getShadowTracePerformance() { return perf(stats().num_shadow_rays, getShadowTraceTime()); }
+    float getPathTracePerformance() { return perf(stats().num_path_rays, getPathTraceTime()); }
+    float getTracePerformance() { return perf(getNumberOfRays(), getTraceTime()); }
+    /* Mrays/s of the last frame over all rays against the whole frame's
+     * device time (no counterpart: the reference divides by trace time). */
+    float getFramePerformance() {
+        const wfpt_render_stats s = stats();
+        return perf(s.num_primary_rays + s.num_shadow_rays + s.num_path_rays, s.frame_ms);
+    }
+    /* Renderer::getShadowSortLogs / getPathSortLogs (Renderer.cpp:708-714). */
+    wfpt_sort_log getShadowSortLog(int depth) { return stats().shadow_sort_logs[depth]; }
+    wfpt_sort_log getPathSortLog(int depth) { return stats().path_sort_logs[depth]; }
     wfpt_renderer* get() const { return r_; }
 
 private:
+    static float perf(unsigned long long rays, float ms) { return ms == 0.0f ? 0.0f : (float)(rays * 1.0e-3 / ms); }
     wfpt_renderer* r_ = nullptr;
 };
 

@@ -23,7 +23,7 @@ class FrameCfg(C.Structure):
                 ("radius", C.c_float), ("key", C.c_float), ("white", C.c_float), ("albedo", C.c_float),
                 ("sort_shadow", C.c_int), ("reorder_shadow", C.c_int), ("sort_path", C.c_int),
                 ("reorder_path", C.c_int), ("morton_kind", C.c_int), ("frame_index", C.c_int),
-                ("path_sort_skip", C.c_int)]
+                ("path_sort_skip", C.c_int), ("accumulate_fp64", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -272,12 +272,30 @@ class Fp64Scene:
 
 
 def render_frame(nodes, tris, geom: HostGeometry, smin, smax, light, bg, s2w, eye, zfar, w, h, cfg: FrameCfg,
-                 pixels=None):
+                 pixels=None, accum=None):
+    """One frame of Renderer::render.  With cfg.accumulate_fp64 the running
+    mean lives in `accum` (float64 [w*h, 4], updated in place; allocated
+    when None and returned as a fourth value)."""
     n = w * h
     px = np.zeros((n, 4), np.float32) if pixels is None else np.ascontiguousarray(pixels, np.float32).copy()
     fp = np.zeros((n, 4), np.float32)
     st = Stats()
+    if cfg.accumulate_fp64 and accum is None:
+        accum = np.zeros((n, 4), np.float64)
     _call(load().orc_render_frame, ptr(nodes), ptr(tris), ptr(geom.table), ptr(_f(smin, 3)), ptr(_f(smax, 3)),
                             ptr(_f(light, 3)), ptr(_f(bg, 3)), ptr(_f(s2w, 16)), ptr(_f(eye, 3)), C.c_float(zfar),
-                            C.c_int(w), C.c_int(h), C.byref(cfg), ptr(px), ptr(fp), C.byref(st))
+                            C.c_int(w), C.c_int(h), C.byref(cfg), ptr(px), ptr(fp), C.byref(st),
+                            ptr(accum) if cfg.accumulate_fp64 else None)
+    if cfg.accumulate_fp64:
+        return px, fp, st, accum
     return px, fp, st
+
+
+def interpolate_colors_fp64(frame_pixels, pixels, accum, frame_index, key, white):
+    """Returns (frame_pixels, pixels, accum) after one FP64 running-mean step."""
+    fp = np.ascontiguousarray(frame_pixels, np.float32).copy()
+    pp = np.ascontiguousarray(pixels, np.float32).copy()
+    acc = np.ascontiguousarray(accum, np.float64).copy()
+    _call(load().orc_interpolate_colors_fp64, ptr(fp), ptr(pp), ptr(acc), C.c_uint32(fp.shape[0]),
+          C.c_int(frame_index), C.c_float(key), C.c_float(white))
+    return fp, pp, acc

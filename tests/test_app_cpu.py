@@ -113,8 +113,19 @@ def test_image_writers(app, tmp_path):
 
 
 def test_benchmark_text(app):
+    log = dict(ray_count=60, morton_ms=0.01, sort_ms=0.02, reorder_ms=0.0, trace_sort_ms=0.1, trace_ms=0.12)
     res = {"ray_type": "path", "total_rays": 100, "primary_rays": 10, "shadow_rays": 60, "path_rays": 30,
-           "render_kernels_ms": 1.5, "render_absolute_ms": 2.0, "rt_perf_total_mrays_s": 66.67}
+           "render_kernels_ms": 1.5, "render_absolute_ms": 2.0, "trace_total_ms": 1.2, "trace_primary_ms": 0.2,
+           "trace_shadow_ms": 0.6, "trace_path_ms": 0.4, "rt_perf_total_mrays_s": 83.33,
+           "rt_perf_primary_mrays_s": 50.0, "rt_perf_shadow_mrays_s": 100.0, "rt_perf_path_mrays_s": 75.0,
+           "print_sort_logs": True, "shadow_sort_logs": [log, log], "path_sort_logs": [dict(log, ray_count=30)]}
     t = app.benchmark_text(res)
     assert " RAY TRACING BENCHMARK RESULTS " in t and " TOTAL RAYS              : 100" in t
-    assert " RT PERF TOTAL           : 66.67" in t
+    for line in (" TRACE TOTAL             : 1.2000 ms", " TRACE SHADOW            : 0.6000 ms",
+                 " RT PERF TOTAL           : 83.33", " RT PERF PRIMARY         : 50.00",
+                 " RT PERF SHADOW          : 100.00", " RT PERF PATH            : 75.00",
+                 "SORT LOG SHADOW AT DEPTH 1", "SORT LOG PATH AT DEPTH 1", "SORT LOG SHADOW TOTAL"):
+        assert line in t, line
+    total = t[t.index("SORT LOG SHADOW TOTAL"):]
+    assert "RAY COUNTS        : 120" in total and "TRACE TIME        : 0.2400 ms" in total
+    assert "SORT LOG" not in app.benchmark_text(dict(res, print_sort_logs=False))

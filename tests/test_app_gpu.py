@@ -35,6 +35,15 @@ def test_env_run_matches_direct_renderer(wf, dev, tmp_path):
     opts = app.load_env(ENV)
     res = app.run(opts, str(tmp_path / "out.pfm"), device=dev, quiet=True)
     assert res["frames"] == 3 and res["total_rays"] > 64 * 48
+    # Benchmark mode times every stage: trace times per ray type, RT PERF
+    # from them (not from the frame time), sort logs of the sorted bounces.
+    assert res["stage_times"]
+    assert 0 < res["trace_total_ms"] < res["render_kernels_ms"]
+    for k in ("primary", "shadow", "path"):
+        assert res[f"trace_{k}_ms"] > 0 and res[f"rt_perf_{k}_mrays_s"] > 0
+    assert res["rt_perf_total_mrays_s"] > res["frame_perf_mrays_s"]
+    assert res["path_sort_logs"][0]["sort_ms"] > 0 and res["path_sort_logs"][0]["ray_count"] > 0
+    assert "RT PERF PATH" in app.benchmark_text(res)
     img = app.read_pfm(tmp_path / "out.pfm")
     pos, nrm, idx = wf.api.generate_scene(0, 5, 3000)
     sc = wf.api.Scene(pos, idx)

@@ -233,3 +233,163 @@ def test_full_size_frames_identical_across_forms(wf, dev, workload):
         assert c == counts
         assert np.array_equal(got, ref)
     assert wf.api.device_status() == 0
+
+
+def _workload_frame_vs_oracle(wf, orc, dev, W, w, h, form, cfg_over=None):
+    """One frame of a benchmark workload rendered by the GPU renderer in
+    `form` and by the oracle's CPU frame (FP32 BVH2 traversal, the
+    reference's pass order and batch cap), compared pixel by pixel (tone
+    mapped and accumulated) and in every ray count."""
+    import sys
+    from pathlib import Path
+
+    import torch
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+    pos, nrm, idx = wf.api.generate_scene(W["scene_kind"], W["seed"])
+    sc = wf.api.Scene(pos, idx)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    rcfg = dict(bench.COURTYARD["renderer"], **W["renderer"])
+    rcfg.update(cfg_over or {})
+    rcfg.update(form)
+    r = wf.api.Renderer(**rcfg)
+    r.set_scene(sc, geom, W["light"], W["background"])
+    cam = wf.api.make_camera(**W["camera"])
+    px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+    r.render(cam, w, h, px, fp)
+    st = r.stats()
+    g_px, g_fp = N(px), N(fp)
+    r.close()
+    assert wf.api.device_status() == 0
+    nodes, tris = sc.export_bvh2()
+    hg = orc.HostGeometry(wf.api.gltf_vertices(pos, nrm), idx)
+    c = W["camera"]
+    s2w = wf.api.camera_screen_to_world(c["position"], c["rotation_deg"], c["fov_deg"], w / h, c["znear"], c["zfar"])
+    cfg = orc.FrameCfg(ray_type=rcfg["ray_type"], spp=rcfg["num_primary_samples"], S=rcfg["num_shadow_samples"],
+                       depth=rcfg["recursion_depth"], radius=rcfg["shadow_radius"], key=rcfg["key_value"],
+                       white=rcfg["white_point"], albedo=rcfg["albedo"], sort_shadow=rcfg.get("sort_shadow_rays", 0),
+                       reorder_shadow=rcfg.get("reorder_shadow_rays", 0), sort_path=rcfg.get("sort_path_rays", 0),
+                       reorder_path=rcfg.get("reorder_path_rays", 0), morton_kind=rcfg.get("morton_kind", 0),
+                       frame_index=1, path_sort_skip=rcfg.get("path_sort_skip", 0))
+    o_px, o_fp, o_st = orc.render_frame(nodes, tris, hg, sc.bounds_min, sc.bounds_max, W["light"], W["background"],
+                                        s2w, c["position"], c["zfar"], w, h, cfg)
+    sc.close()
+    assert st.num_primary_rays == o_st.primary
+    assert st.num_shadow_rays == o_st.shadow
+    assert st.num_path_rays == o_st.path
+    assert list(st.path_rays_per_bounce) == list(o_st.path_per_bounce)
+    assert same_bits(g_fp, o_fp) and same_bits(g_px, o_px)
+    return st
+
+
+def test_courtyard_1080p_chosen_frame_matches_oracle(wf, orc, dev):
+    """The benchmark frame itself: courtyard, 1920x1080, 8 bounces, chosen
+    form (BVH8-Q8, 6-D 64-bit Morton sort + reorder of every bounce's path
+    rays, graph replay, overlapped shadow passes) against the oracle frame,
+    bit for bit."""
+    import bench
+    st = _workload_frame_vs_oracle(wf, orc, dev, bench.COURTYARD, 1920, 1080, bench.CHOSEN)
+    assert st.num_path_rays > 10_000_000
+
+
+def test_city_frame_matches_oracle(wf, orc, dev):
+    """The 3,000,320-triangle city block at 960x540 (a sixteenth of its
+    benchmark pixels; the BVH, scene and camera are the benchmark's), chosen
+    form, against the oracle frame, bit for bit."""
+    import bench
+    _workload_frame_vs_oracle(wf, orc, dev, bench.CITY, 960, 540, bench.CHOSEN)
+
+
+@pytest.mark.parametrize("overlap", [0, 1])
+def test_multi_batch_shadow_frame_matches_oracle(wf, orc, dev, overlap):
+    """A frame whose primary shadow pass needs two batches under the
+    reference's cap of 8M rays per batch (1024x1024 pixels x 9 shadow
+    samples = 9.4M rays: batches of 932,067 and 116,509 inputs, each batch's
+    seeds indexed from its own start as raygenShadow.comp:85 does), the
+    bounces one batch each, against the oracle frame."""
+    import bench
+    st = _workload_frame_vs_oracle(wf, orc, dev, bench.COURTYARD, 1024, 1024,
+                                   dict(bench.CHOSEN, shadow_overlap=overlap),
+                                   cfg_over=dict(num_shadow_samples=9, recursion_depth=2))
+    assert st.num_primary_rays * 9 > 8 * 1024 * 1024
+
+
+def test_fp64_accumulation_frames_match_oracle(wf, orc, dev, small):
+    """accumulate_fp64: four frames (graph replay), each frame's pixels and
+    tone-mapped image bit-exact against the oracle keeping the same double
+    running mean; frame 1 equals the float mode's."""
+    import torch
+    sc, geom, nodes, tris, hg = small
+    w, h = 64, 48
+    base = dict(ray_type=wf.PATH_RAYS, num_primary_samples=1, num_shadow_samples=2, shadow_radius=0.1,
+                recursion_depth=3, key_value=0.6, white_point=2.0, bvh_kind=wf.BVH8_Q8, albedo=0.8, use_graph=1,
+                sort_path_rays=1, reorder_path_rays=1, morton_kind=2)
+    r = wf.api.Renderer(accumulate_fp64=1, **base)
+    r.set_scene(sc, geom, LIGHT, BG)
+    cam = wf.api.make_camera(**CAM)
+    px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+    fp = torch.zeros_like(px)
+    s2w = wf.api.camera_screen_to_world(CAM["position"], CAM["rotation_deg"], CAM["fov_deg"], w / h, CAM["znear"],
+                                        CAM["zfar"])
+    cfg = orc.FrameCfg(ray_type=2, spp=1, S=2, depth=3, radius=0.1, key=0.6, white=2.0, albedo=0.8, sort_path=1,
+                       reorder_path=1, morton_kind=2, frame_index=1, accumulate_fp64=1)
+    o_px, acc = None, None
+    for f in range(1, 5):
+        r.render(cam, w, h, px, fp)
+        cfg.frame_index = f
+        o_px, o_fp, _, acc = orc.render_frame(nodes, tris, hg, sc.bounds_min, sc.bounds_max, LIGHT, BG, s2w,
+                                              CAM["position"], CAM["zfar"], w, h, cfg, pixels=o_px, accum=acc)
+        assert same_bits(N(fp), o_fp) and same_bits(N(px), o_px), f
+        if f == 1:
+            r32 = wf.api.Renderer(**base)
+            r32.set_scene(sc, geom, LIGHT, BG)
+            px32, fp32 = torch.zeros_like(px), torch.zeros_like(px)
+            r32.render(cam, w, h, px32, fp32)
+            assert same_bits(N(px32), N(px))
+    assert wf.api.device_status() == 0
+
+
+def test_timing_stats_fill_trace_times_and_sort_logs(wf, dev, small):
+    """timing=1 (the reference's benchmark mode with printSortLogs): the
+    frame is unchanged (pixels and ray counts equal the graph-replayed,
+    overlapped frame's), the per-type trace times are positive and add up to
+    less than the frame, and every sorted pass has a sort log with its
+    Morton, sort, reorder, sorted-trace and unsorted-trace times."""
+    import torch
+    sc, geom, nodes, tris, hg = small
+    w, h = 128, 96
+    base = dict(ray_type=wf.PATH_RAYS, num_primary_samples=2, num_shadow_samples=2, shadow_radius=0.1,
+                recursion_depth=4, key_value=0.6, white_point=2.0, bvh_kind=wf.BVH8_Q8, albedo=0.8,
+                sort_path_rays=1, reorder_path_rays=1, morton_kind=2, sort_shadow_rays=1, reorder_shadow_rays=0,
+                use_graph=1, shadow_overlap=1, path_sort_skip=0b0010)
+    out = []
+    for timing in (0, 1):
+        r = wf.api.Renderer(timing=timing, **base)
+        r.set_scene(sc, geom, LIGHT, BG)
+        px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+        fp = torch.zeros_like(px)
+        r.render(wf.api.make_camera(**CAM), w, h, px, fp)
+        out.append((N(px), N(fp), r.stats()))
+        r.close()
+    (pa, fa, s0), (pb, fb, st) = out
+    assert same_bits(pa, pb) and same_bits(fa, fb)
+    assert (s0.num_primary_rays, s0.num_shadow_rays, s0.num_path_rays) == \
+        (st.num_primary_rays, st.num_shadow_rays, st.num_path_rays)
+    assert s0.timed == 0 and s0.primary_trace_ms == 0.0
+    assert st.timed == 1
+    assert st.primary_trace_ms > 0 and st.shadow_trace_ms > 0 and st.path_trace_ms > 0
+    assert st.primary_trace_ms + st.shadow_trace_ms + st.path_trace_ms < st.frame_ms
+    for b in range(4):
+        lg = st.path_sort_logs[b]
+        assert lg.ray_count == st.path_rays_per_bounce[b] > 0
+        if b == 1:  # path_sort_skip: bounce 2 traces unsorted, no sort-log times
+            assert lg.morton_ms == lg.sort_ms == lg.trace_sort_ms == lg.trace_ms == 0.0
+        else:
+            assert min(lg.morton_ms, lg.sort_ms, lg.reorder_ms, lg.trace_sort_ms, lg.trace_ms) > 0
+    for i in range(5):
+        lg = st.shadow_sort_logs[i]
+        assert lg.ray_count == 2 * st.shadow_hits_per_pass[i]
+        assert lg.reorder_ms == 0.0  # shadow rays sorted, traced through the indirect index
+        assert min(lg.morton_ms, lg.sort_ms, lg.trace_sort_ms, lg.trace_ms) > 0
+    assert wf.api.device_status() == 0

@@ -299,3 +299,50 @@ def test_reorder_full_size_properties(wf, dev):
     assert torch.equal(os2i, s2i[li])
     slots = torch.arange(n, dtype=torch.int32, device=dev)
     assert torch.equal(oi2s[os2i.to(torch.int64)], slots)
+
+
+def test_interpolate_colors_fp64_matches_oracle(wf, orc, dev):
+    """The FP64 running mean over five frames, bit-exact against the
+    oracle's double evaluation (pixels, tone-mapped frame and the double
+    accumulator itself)."""
+    import torch
+    rng = np.random.default_rng(31)
+    n = 30001
+    pp = np.zeros((n, 4), np.float32)
+    acc = np.zeros((n, 4), np.float64)
+    d_pp = T(pp, dev)
+    d_acc = torch.zeros((n, 4), dtype=torch.float64, device=dev)
+    for frame in range(1, 6):
+        fp = rng.uniform(0, 3, (n, 4)).astype(np.float32)
+        fp[:5] = 0.0
+        d_fp = T(fp, dev)
+        wf.api.interpolate_colors_fp64(d_fp, d_pp, d_acc, frame, 0.6, 2.0)
+        r_fp, pp, acc = orc.interpolate_colors_fp64(fp, pp, acc, frame, 0.6, 2.0)
+        got_fp = N(d_fp)
+        assert np.array_equal(np.isnan(got_fp), np.isnan(r_fp))
+        assert np.array_equal(bits(np.nan_to_num(got_fp)), bits(np.nan_to_num(r_fp)))
+        assert np.array_equal(bits(N(d_pp)), bits(pp))
+        assert np.array_equal(N(d_acc).view(np.uint64), acc.view(np.uint64))
+
+
+def test_fp64_accumulation_tracks_the_exact_mean(wf, dev):
+    """Over 512 frames of random colours, the FP64 running mean stays within
+    one float rounding of the exact mean of the frames, while the float
+    running mean of interpolateColors.comp drifts much further."""
+    import torch
+    rng = np.random.default_rng(32)
+    n, frames = 4096, 512
+    d_pp32 = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    d_pp64 = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    d_acc = torch.zeros((n, 4), dtype=torch.float64, device=dev)
+    total = np.zeros((n, 3), np.float64)
+    for f in range(1, frames + 1):
+        fp = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+        total += fp[:, :3]
+        wf.api.interpolate_colors(T(fp, dev), d_pp32, f, 0.6, 2.0)
+        wf.api.interpolate_colors_fp64(T(fp, dev), d_pp64, d_acc, f, 0.6, 2.0)
+    exact = total / frames
+    err32 = np.abs(N(d_pp32)[:, :3].astype(np.float64) - exact).max()
+    err64 = np.abs(N(d_pp64)[:, :3].astype(np.float64) - exact).max()
+    assert err64 <= 2.0**-24  # the mean is below 1: half an ulp of the float result
+    assert err32 > 16 * err64

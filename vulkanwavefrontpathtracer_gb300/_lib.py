@@ -71,6 +71,8 @@ class RendererConfig(C.Structure):
         ("path_sort_skip", c_int),
         ("shadow_overlap", c_int),
         ("primary_bvh_kind", c_int),
+        ("timing", c_int),
+        ("accumulate_fp64", c_int),
     ]
 
 
@@ -84,6 +86,17 @@ class Camera(C.Structure):
     ]
 
 
+class SortLog(C.Structure):
+    _fields_ = [
+        ("ray_count", c_u64),
+        ("morton_ms", c_float),
+        ("sort_ms", c_float),
+        ("reorder_ms", c_float),
+        ("trace_sort_ms", c_float),
+        ("trace_ms", c_float),
+    ]
+
+
 class RenderStats(C.Structure):
     _fields_ = [
         ("num_primary_rays", c_u64),
@@ -92,6 +105,12 @@ class RenderStats(C.Structure):
         ("path_rays_per_bounce", c_u32 * 8),
         ("shadow_hits_per_pass", c_u32 * 9),
         ("frame_ms", c_float),
+        ("timed", c_int),
+        ("primary_trace_ms", c_float),
+        ("shadow_trace_ms", c_float),
+        ("path_trace_ms", c_float),
+        ("shadow_sort_logs", SortLog * 9),
+        ("path_sort_logs", SortLog * 8),
     ]
 
 
@@ -156,6 +175,8 @@ _SIGS = {
                                         c_int, c_int, c_void_p]),
     "wfpt_count_hits": (c_int, [c_void_p, c_u32, c_void_p, c_void_p, c_void_p]),
     "wfpt_interpolate_colors": (c_int, [c_void_p, c_void_p, c_u32, c_int, c_float, c_float, c_void_p]),
+    "wfpt_interpolate_colors_fp64": (c_int, [c_void_p, c_void_p, c_void_p, c_u32, c_int, c_float, c_float,
+                                             c_void_p]),
     "wfpt_fill_u32": (c_int, [c_void_p, c_u32, c_size_t, c_void_p]),
     "wfpt_scene_create": (c_int, [c_void_p, c_u32, c_void_p, c_u32, c_void_p, c_u32, c_int, C.POINTER(c_void_p)]),
     "wfpt_scene_create_device": (c_int, [c_void_p, c_u32, c_void_p, c_u32, c_void_p, c_u32, c_int, c_void_p,

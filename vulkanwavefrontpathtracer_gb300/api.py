@@ -223,6 +223,15 @@ def interpolate_colors(frame_pixels, pixels, frame_index, key_value, white_point
                                           white_point, _s(stream)))
 
 
+def interpolate_colors_fp64(frame_pixels, pixels, accum, frame_index, key_value, white_point, n=None, stream=None):
+    """interpolate_colors with the running mean in double: accum is a
+    float64 tensor of 4 values per pixel (xyz the mean), kept across frames."""
+    if accum.dtype != torch.float64 or accum.numel() < 4 * _n(pixels, n):
+        raise ValueError("accum must be a float64 tensor of 4 values per pixel")
+    L.check(lib().wfpt_interpolate_colors_fp64(_p(frame_pixels), _p(pixels), _p(accum), _n(pixels, n), frame_index,
+                                               key_value, white_point, _s(stream)))
+
+
 def fill_u32(dst, pattern: int, count: int, stream=None):
     L.check(lib().wfpt_fill_u32(_p(dst), pattern & 0xFFFFFFFF, count, _s(stream)))
 

@@ -19,6 +19,15 @@ Options beyond the reference (same file, same style):
                           primary pass (camera rays and their shadow rays)
   Renderer.shadowOverlap  bool: trace each pass's shadow rays concurrently with
                           the next bounce (default true; same image)
+  Renderer.accumulateFp64 bool: keep the running mean over frames in double
+                          (default false: float, as interpolateColors.comp)
+  Benchmark.stageTimes    bool (default true): in benchmark mode, time every
+                          stage with CUDA events (the frame is launched
+                          directly on one stream), which gives the TRACE
+                          times, RT PERF per ray type (rays / trace time, as
+                          the reference) and the SORT LOG; false: graph
+                          replay and overlap as configured, RENDER KERNELS
+                          only
   Benchmark.warmupCycles  int                          (default 3)
   Benchmark.benchmarkCycles int                        (default 10)
   Scene.generator         "soup:<triangles>:<seed>" | "courtyard[:<seed>]" |
@@ -48,6 +57,7 @@ DEFAULTS: Dict[str, Any] = {
     "Benchmark.printSortLogs": False,
     "Benchmark.warmupCycles": 3,
     "Benchmark.benchmarkCycles": 10,
+    "Benchmark.stageTimes": True,
     "Resolution.width": 1024,
     "Resolution.height": 768,
     "Scene.filename": "",
@@ -74,6 +84,7 @@ DEFAULTS: Dict[str, Any] = {
     "Renderer.pathSortSkip": 0,
     "Renderer.shadowOverlap": True,
     "Renderer.primaryBvh": "",
+    "Renderer.accumulateFp64": False,
     "Camera.position": [0.0, 0.0, 0.0],
     "Camera.rotation": [0.0, 0.0, 0.0],
     "Camera.nearPlane": 0.001,
@@ -166,7 +177,9 @@ def renderer_config(opts: Dict[str, Any]):
         use_graph=1 if opts["Renderer.useGraph"] else 0,
         path_sort_skip=opts["Renderer.pathSortSkip"],
         shadow_overlap=1 if opts["Renderer.shadowOverlap"] else 0,
-        primary_bvh_kind=-1 if opts["Renderer.primaryBvh"] == "" else BVH_KINDS[opts["Renderer.primaryBvh"]])
+        primary_bvh_kind=-1 if opts["Renderer.primaryBvh"] == "" else BVH_KINDS[opts["Renderer.primaryBvh"]],
+        timing=1 if opts["Application.mode"] == "benchmark" and opts["Benchmark.stageTimes"] else 0,
+        accumulate_fp64=1 if opts["Renderer.accumulateFp64"] else 0)
 
 
 # ------------------------------------------------------------ scene input
@@ -318,24 +331,54 @@ def run(opts: Dict[str, Any], out_image: str = "", device=None, frames=None, qui
     cycles = opts["Benchmark.benchmarkCycles"] if frames is None else frames
     if opts["Application.mode"] != "benchmark" and frames is None:
         warm, cycles = 0, 1
-    acc = dict(kernels_ms=0.0, absolute_ms=0.0, rays=0, primary=0, shadow=0, path=0)
+    keys = ("primary", "shadow", "path")
+    acc = dict(kernels_ms=0.0, absolute_ms=0.0, primary=0, shadow=0, path=0, trace_primary=0.0, trace_shadow=0.0,
+               trace_path=0.0, perf_total=0.0, perf_primary=0.0, perf_shadow=0.0, perf_path=0.0)
+    depth = opts["Renderer.recursionDepth"]
+    fields = ("ray_count", "morton_ms", "sort_ms", "reorder_ms", "trace_sort_ms", "trace_ms")
+    shadow_logs = [dict.fromkeys(fields, 0.0) for _ in range(depth + 1)]
+    path_logs = [dict.fromkeys(fields, 0.0) for _ in range(depth)]
+    timed = False
+
+    def perf(rays, ms):  # Renderer::get*TracePerformance (Renderer.cpp:692-706)
+        return rays * 1.0e-3 / ms if ms > 0 else 0.0
+
     for f in range(warm + cycles):
         t = time.perf_counter()
         r.render(cam, w, h, px, fp)
         st = r.stats()  # waits for the frame
         absolute = (time.perf_counter() - t) * 1e3
-        if f >= warm:
-            acc["kernels_ms"] += st.frame_ms
-            acc["absolute_ms"] += absolute
-            acc["primary"] += st.num_primary_rays
-            acc["shadow"] += st.num_shadow_rays
-            acc["path"] += st.num_path_rays
+        if f < warm:
+            continue
+        timed = bool(st.timed)
+        acc["kernels_ms"] += st.frame_ms
+        acc["absolute_ms"] += absolute
+        counts = (st.num_primary_rays, st.num_shadow_rays, st.num_path_rays)
+        times = (st.primary_trace_ms, st.shadow_trace_ms, st.path_trace_ms)
+        for k, c, ms in zip(keys, counts, times):
+            acc[k] += c
+            acc["trace_" + k] += ms
+            acc["perf_" + k] += perf(c, ms)
+        acc["perf_total"] += perf(sum(counts), sum(times))
+        for logs, src in ((shadow_logs, st.shadow_sort_logs), (path_logs, st.path_sort_logs)):
+            for i, lg in enumerate(logs):
+                for fld in fields:
+                    lg[fld] += getattr(src[i], fld)
     n = max(cycles, 1)
     rays = (acc["primary"] + acc["shadow"] + acc["path"]) / n
     res = {"ray_type": opts["Renderer.rayType"], "total_rays": rays, "primary_rays": acc["primary"] / n,
            "shadow_rays": acc["shadow"] / n, "path_rays": acc["path"] / n,
            "render_kernels_ms": acc["kernels_ms"] / n, "render_absolute_ms": acc["absolute_ms"] / n,
-           "rt_perf_total_mrays_s": rays * 1e-3 / (acc["kernels_ms"] / n) if acc["kernels_ms"] else 0.0,
+           "stage_times": timed,
+           "trace_total_ms": (acc["trace_primary"] + acc["trace_shadow"] + acc["trace_path"]) / n,
+           "trace_primary_ms": acc["trace_primary"] / n, "trace_shadow_ms": acc["trace_shadow"] / n,
+           "trace_path_ms": acc["trace_path"] / n,
+           "rt_perf_total_mrays_s": acc["perf_total"] / n, "rt_perf_primary_mrays_s": acc["perf_primary"] / n,
+           "rt_perf_shadow_mrays_s": acc["perf_shadow"] / n, "rt_perf_path_mrays_s": acc["perf_path"] / n,
+           "frame_perf_mrays_s": rays * 1e-3 / (acc["kernels_ms"] / n) if acc["kernels_ms"] else 0.0,
+           "shadow_sort_logs": [{k: v / n for k, v in lg.items()} for lg in shadow_logs],
+           "path_sort_logs": [{k: v / n for k, v in lg.items()} for lg in path_logs],
+           "print_sort_logs": bool(opts["Benchmark.printSortLogs"]),
            "frames": warm + cycles, "bvh_build_ms": build_ms, "triangles": int(idx.shape[0])}
     if out_image:
         img = pixels_to_image(px.cpu().numpy(), w, h)
@@ -347,19 +390,48 @@ def run(opts: Dict[str, Any], out_image: str = "", device=None, frames=None, qui
 
 
 def benchmark_text(res: Dict[str, Any]) -> str:
-    """The results block of Benchmark::run (Benchmark.cpp:128-156); the
-    trace time is the frame's device time (all kernels)."""
+    """The results block of Benchmark::run (Benchmark.cpp:128-195): averaged
+    counts, TRACE times and RT PERF per ray type (rays / trace time, where a
+    trace time covers ray generation, sorting and traversal as in the
+    reference; zero without stage times), the overall times, and with
+    Benchmark.printSortLogs the SORT LOG of every depth and its total."""
     lines = [
         "=" * 50, " RAY TRACING BENCHMARK RESULTS ", "-" * 50,
         f" RAY TYPE                : {res['ray_type']}", "", " [Count (Average)]",
         f" TOTAL RAYS              : {int(res['total_rays'])}",
         f" PRIMARY RAYS            : {int(res['primary_rays'])}",
         f" SHADOW RAYS             : {int(res['shadow_rays'])}",
-        f" PATH RAYS               : {int(res['path_rays'])}", "", " [Performance (Mrays/s)]",
-        f" RT PERF TOTAL           : {res['rt_perf_total_mrays_s']:.2f}", "", " [Overall Time]",
+        f" PATH RAYS               : {int(res['path_rays'])}", "", " [Time (ms)]",
+        f" TRACE TOTAL             : {res['trace_total_ms']:.4f} ms",
+        f" TRACE PRIMARY           : {res['trace_primary_ms']:.4f} ms",
+        f" TRACE SHADOW            : {res['trace_shadow_ms']:.4f} ms",
+        f" TRACE PATH              : {res['trace_path_ms']:.4f} ms", "", " [Performance (Mrays/s)]",
+        f" RT PERF TOTAL           : {res['rt_perf_total_mrays_s']:.2f}",
+        f" RT PERF PRIMARY         : {res['rt_perf_primary_mrays_s']:.2f}",
+        f" RT PERF SHADOW          : {res['rt_perf_shadow_mrays_s']:.2f}",
+        f" RT PERF PATH            : {res['rt_perf_path_mrays_s']:.2f}", "", " [Overall Time]",
         f" RENDER KERNELS          : {res['render_kernels_ms']:.4f} ms",
         f" RENDER ABSOLUTE         : {res['render_absolute_ms']:.4f} ms", "-" * 50, "=" * 50]
+    if res.get("print_sort_logs"):
+        for label, logs, first in (("SHADOW", res["shadow_sort_logs"], 0), ("PATH", res["path_sort_logs"], 1)):
+            total = {k: 0.0 for k in ("ray_count", "morton_ms", "sort_ms", "reorder_ms", "trace_sort_ms",
+                                      "trace_ms")}
+            lines += ["=" * 50, "-" * 50]
+            for i, lg in enumerate(logs):
+                lines += [f"SORT LOG {label} AT DEPTH {i + first}", *_sort_log_lines(lg), ""]
+                for k in total:
+                    total[k] += lg[k]
+            lines += ["-" * 50, f"SORT LOG {label} TOTAL", *_sort_log_lines(total), "-" * 50, "=" * 50]
     return "\n".join(lines)
+
+
+def _sort_log_lines(lg: Dict[str, float]) -> List[str]:
+    return [f"RAY COUNTS        : {int(lg['ray_count'])}",
+            f"MORTONCODES TIME  : {lg['morton_ms']:.4f} ms",
+            f"SORT TIME         : {lg['sort_ms']:.4f} ms",
+            f"REORDER TIME      : {lg['reorder_ms']:.4f} ms",
+            f"TRACE SORT TIME   : {lg['trace_sort_ms']:.4f} ms",
+            f"TRACE TIME        : {lg['trace_ms']:.4f} ms\n"]
 
 
 def main(argv: List[str] = None) -> int:

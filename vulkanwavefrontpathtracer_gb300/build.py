@@ -42,7 +42,9 @@ def headers() -> list[Path]:
 def _compile(src: Path, obj: Path, verbose: bool, ptxas_v: bool) -> tuple[Path, str]:
     cmd = [nvcc(), *ARCH, *COMMON, "-c", str(src), "-o", str(obj), "-I", str(INCLUDE)]
     if src.suffix == ".cpp":
-        cmd += ["-Xcompiler", "-pthread"]
+        # Host code rounds every float operation as written (no FMA
+        # contraction), so that x86 and Arm hosts compute the same bits.
+        cmd += ["-Xcompiler", "-pthread", "-Xcompiler", "-ffp-contract=off"]
     if ptxas_v and src.suffix == ".cu":
         cmd += ["-Xptxas", "-v"]
     if verbose:

@@ -449,6 +449,15 @@ wfpt_status wfpt_interpolate_colors(float* frame_pixels, float* pixels, uint32_t
         wfpt::launch_interpolate_colors(frame_pixels, pixels, num_pixels, frame_index, key_value, white_point, S(stream)));
 }
 
+wfpt_status wfpt_interpolate_colors_fp64(float* frame_pixels, float* pixels, double* accum, uint32_t num_pixels,
+                                         int frame_index, float key_value, float white_point, void* stream) {
+    WFPT_REQUIRE(num_pixels <= kMaxN, "too many pixels");
+    WFPT_REQUIRE(num_pixels == 0 || (frame_pixels && pixels && accum), "null buffer");
+    WFPT_REQUIRE(reinterpret_cast<uintptr_t>(accum) % 32 == 0, "accum must be 32-byte aligned");
+    return from_cuda(wfpt::launch_interpolate_colors_fp64(frame_pixels, pixels, accum, num_pixels, frame_index,
+                                                          key_value, white_point, S(stream)));
+}
+
 wfpt_status wfpt_fill_u32(void* dst, uint32_t pattern, size_t count_u32, void* stream) {
     WFPT_REQUIRE(count_u32 == 0 || dst, "null buffer");
     return from_cuda(wfpt::launch_fill_u32(dst, pattern, count_u32, S(stream)));

@@ -66,18 +66,19 @@ void pixel_table(int width, int height, int32_t* idx_to_pix, int32_t* pix_to_idx
 // ------------------------------------------------------------------ camera
 namespace {
 struct V3 {
-    double x, y, z;
+    float x, y, z;
 };
-V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+V3 cross(V3 a, V3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
 V3 nrm(V3 a) {
-    double l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
     return {a.x / l, a.y / l, a.z / l};
 }
-// camera.hpp:47-64: rotate v about u, then n = u x v.
-void rotate_axis(double ang, V3* u, V3* v, V3* n) {
-    double s = std::sin(ang), c = std::cos(ang);
+// camera.hpp:47-64: v = normalize(v cos + (u x v) sin), n = normalize(u x v).
+void rotate_axis(float ang, V3* u, V3* v, V3* n) {
+    float s = std::sin(ang), c = std::cos(ang);
     V3 uv = cross(*u, *v);
-    *v = nrm({v->x * c + uv.x * s, v->y * c + uv.y * s, v->z * c + uv.z * s});
+    V3 t{v->x * c + uv.x * s, v->y * c + uv.y * s, v->z * c + uv.z * s};
+    *v = nrm(t);
     *n = nrm(cross(*u, *v));
 }
 bool invert4(const double m[16], double out[16]) {
@@ -110,39 +111,36 @@ bool invert4(const double m[16], double out[16]) {
 }  // namespace
 
 // inverse(P * V): camera.hpp:23-45 (view from Euler angles, applied in the
-// order y, x, z) and :108-120 (perspective, right-handed, depth 0..1,
-// P[1][1] negated), RayGen.cpp:93.  Evaluated in double, rounded to float.
+// order y, x, z; view = translate(transpose(rot), -position)) and :108-120
+// (perspective, right-handed, depth 0..1, P[1][1] negated), RayGen.cpp:93.
+// V, P and their product are evaluated in float in the camera header's
+// operation order, as the reference's glm float matrices are (this file is
+// compiled without FMA contraction); the product is inverted in double and
+// rounded to float.
 bool camera_screen_to_world(const float pos[3], const float rot_deg[3], float fov_deg, float aspect, float znear,
                             float zfar, float out[16]) {
-    const double d2r = 3.14159265358979323846 / 180.0;
+    const float d2r = static_cast<float>(3.14159265358979323846 / 180.0);
     V3 u{1, 0, 0}, v{0, 1, 0}, n{0, 0, 1};
-    if (rot_deg[1] != 0.0f) rotate_axis(rot_deg[1] * d2r, &v, &n, &u);
-    if (rot_deg[0] != 0.0f) rotate_axis(rot_deg[0] * d2r, &u, &v, &n);
-    if (rot_deg[2] != 0.0f) rotate_axis(rot_deg[2] * d2r, &n, &u, &v);
-    // view = transpose(mat4(u, v, n, e3)) * translate(-pos); column-major.
-    double V[16] = {0};
-    V[0] = u.x; V[4] = u.y; V[8] = u.z;
-    V[1] = v.x; V[5] = v.y; V[9] = v.z;
-    V[2] = n.x; V[6] = n.y; V[10] = n.z;
-    V[15] = 1.0;
-    double px = pos[0], py = pos[1], pz = pos[2];
-    V[12] = -(u.x * px + u.y * py + u.z * pz);
-    V[13] = -(v.x * px + v.y * py + v.z * pz);
-    V[14] = -(n.x * px + n.y * py + n.z * pz);
-    double th = std::tan(fov_deg * d2r / 2.0);
-    double P[16] = {0};
-    P[0] = 1.0 / (aspect * th);
-    P[5] = -1.0 / th;
-    P[10] = zfar / (znear - zfar);
-    P[11] = -1.0;
-    P[14] = -(zfar * znear) / (zfar - znear);
+    if (rot_deg[1] * d2r != 0.0f) rotate_axis(rot_deg[1] * d2r, &v, &n, &u);
+    if (rot_deg[0] * d2r != 0.0f) rotate_axis(rot_deg[0] * d2r, &u, &v, &n);
+    if (rot_deg[2] * d2r != 0.0f) rotate_axis(rot_deg[2] * d2r, &n, &u, &v);
+    // transpose(mat4(u, v, n, e3)), column-major V[c][r].
+    float V[4][4] = {{u.x, v.x, n.x, 0.0f}, {u.y, v.y, n.y, 0.0f}, {u.z, v.z, n.z, 0.0f}, {0.0f, 0.0f, 0.0f, 1.0f}};
+    // translate(M, -p): column 3 = M0 * -px + M1 * -py + M2 * -pz + M3.
+    const float mp[3] = {-pos[0], -pos[1], -pos[2]};
+    for (int r = 0; r < 4; ++r) V[3][r] = V[0][r] * mp[0] + V[1][r] * mp[1] + V[2][r] * mp[2] + V[3][r];
+    float th = std::tan(fov_deg * d2r / 2.0f);
+    float P[4][4] = {{0.0f}};
+    P[0][0] = 1.0f / (aspect * th);
+    P[1][1] = 1.0f / th;
+    P[2][2] = zfar / (znear - zfar);
+    P[2][3] = -1.0f;
+    P[3][2] = -(zfar * znear) / (zfar - znear);
+    P[1][1] *= -1.0f;
     double PV[16];
     for (int c = 0; c < 4; ++c)
-        for (int r = 0; r < 4; ++r) {
-            double s = 0;
-            for (int k = 0; k < 4; ++k) s += P[k * 4 + r] * V[c * 4 + k];
-            PV[c * 4 + r] = s;
-        }
+        for (int r = 0; r < 4; ++r)
+            PV[c * 4 + r] = P[0][r] * V[c][0] + P[1][r] * V[c][1] + P[2][r] * V[c][2] + P[3][r] * V[c][3];
     double inv[16];
     if (!invert4(PV, inv)) return false;
     for (int i = 0; i < 16; ++i) out[i] = (float)inv[i];

@@ -123,7 +123,37 @@ struct wfpt_renderer {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool shadow_pending = false;
     RayBufferDev primary, shadow, queue[2];
+    DevBuf accum64;  // cfg.accumulate_fp64: the running mean, double4 per pixel
     uint32_t* host_counters = nullptr;  // pinned
+
+    // Timing (cfg.timing, Application.mode "benchmark" with
+    // Benchmark.printSortLogs): a directly launched frame records event
+    // pairs around its stages; get_stats resolves them into the per-type
+    // trace times and the sort logs.  A span counts into a trace-time total
+    // (T_PRIMARY/T_SHADOW/T_PATH) and/or into one component of a sort log
+    // (log 0..8: shadowSortLogs[log], 100 + b: pathSortLogs[b]).
+    enum { T_NONE = -1, T_PRIMARY, T_SHADOW, T_PATH };
+    enum { C_NONE = -1, C_MORTON, C_SORT, C_REORDER, C_TRACE_SORT, C_TRACE };
+    struct Span {
+        int a, b, total, comp, log;
+    };
+    std::vector<cudaEvent_t> tev;
+    size_t tev_used = 0;
+    std::vector<Span> spans;
+    bool timing_on = false;   // the frame being recorded is timed
+    bool last_timed = false;  // the last rendered frame was timed
+
+    // Records the next pool event on s; *idx receives its index.
+    cudaError_t mark(cudaStream_t s, int* idx) {
+        if (tev_used == tev.size()) {
+            cudaEvent_t ev;
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return e;
+            tev.push_back(ev);
+        }
+        *idx = (int)tev_used++;
+        return cudaEventRecord(tev[*idx], s);
+    }
     int last_spp = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     bool stats_pending = false;
@@ -225,6 +255,8 @@ struct wfpt_renderer {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (ev2) cudaEventDestroy(ev2);
+        for (cudaEvent_t ev : tev) cudaEventDestroy(ev);
+        accum64.release();
     }
 
     // Ray counts of the last frame from the counters read back to the host
@@ -248,6 +280,39 @@ struct wfpt_renderer {
                     st->path_rays_per_bounce[b] += c[kCntPath + b];
                 }
         }
+        for (int i = 0; i < 9; ++i) st->shadow_sort_logs[i].ray_count = (uint64_t)S * st->shadow_hits_per_pass[i];
+        for (int b = 0; b < 8; ++b) st->path_sort_logs[b].ray_count = st->path_rays_per_bounce[b];
+    }
+
+    // Trace times and sort-log times of the last frame, when it was timed
+    // (its events have completed: the caller waited for ev2).
+    void fill_times(wfpt_render_stats* st) const {
+        if (!last_timed) return;
+        st->timed = 1;
+        for (const Span& sp : spans) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, tev[sp.a], tev[sp.b]) != cudaSuccess) continue;
+            if (sp.total == T_PRIMARY) st->primary_trace_ms += ms;
+            if (sp.total == T_SHADOW) st->shadow_trace_ms += ms;
+            if (sp.total == T_PATH) st->path_trace_ms += ms;
+            if (sp.comp == C_NONE || sp.log < 0) continue;
+            wfpt_sort_log& lg = sp.log >= 100 ? st->path_sort_logs[sp.log - 100] : st->shadow_sort_logs[sp.log];
+            float* f[5] = {&lg.morton_ms, &lg.sort_ms, &lg.reorder_ms, &lg.trace_sort_ms, &lg.trace_ms};
+            *f[sp.comp] += ms;
+        }
+    }
+
+    // Launches `fn` on s between two timing events when the frame is timed.
+    template <class F>
+    cudaError_t timed(cudaStream_t s, int total, int comp, int log, F&& fn) {
+        if (!timing_on) return fn();
+        int a = 0, b = 0;
+        cudaError_t e;
+        if ((e = mark(s, &a)) != cudaSuccess) return e;
+        if ((e = fn()) != cudaSuccess) return e;
+        if ((e = mark(s, &b)) != cudaSuccess) return e;
+        spans.push_back(Span{a, b, total, comp, log});
+        return cudaSuccess;
     }
 
     int key_bits() const {
@@ -287,6 +352,7 @@ struct wfpt_renderer {
         if ((e = sort_scratch.ensure(wfpt::sort_scratch_bytes((uint32_t)sort_n, 64))) != cudaSuccess) return e;
         if ((e = path_scratch.ensure(wfpt::raygen_path_scratch_bytes((uint32_t)n))) != cudaSuccess) return e;
         if ((e = counters.ensure((size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess) return e;
+        if (cfg.accumulate_fp64 && (e = accum64.ensure(n * 32)) != cudaSuccess) return e;
         if (!work.p) {
             if ((e = work.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
             if ((e = cudaMemset(work.p, 0, work.bytes)) != cudaSuccess) return e;
@@ -315,29 +381,45 @@ struct wfpt_renderer {
 
     // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).  on_side: the
     // launch belongs to the shadow branch (its own counters and scratch).
+    // total / log: where a timed frame books the stages (T_SHADOW or T_PATH;
+    // the sort log slot); a timed sorted pass first traces its rays
+    // unsorted, for the log's trace time, as Renderer.cpp:259-264 and
+    // :281-286 do (the sorted trace then overwrites those results).
     cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
-                           cudaStream_t s, bool on_side, int kind) {
+                           cudaStream_t s, bool on_side, int kind, int total = T_NONE, int log = -1) {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
         uint32_t* wk = on_side ? work_side.as<uint32_t>() : work.as<uint32_t>();
         DevBuf& scratch = on_side ? sort_scratch_side : sort_scratch;
         cudaError_t e;
-        if (!sort) return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n,
-                                             n_dev, closest ? 1 : 0, s, wk);
+        auto plain = [&]() {
+            return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n, n_dev,
+                                      closest ? 1 : 0, s, wk);
+        };
+        if (!sort) return timed(s, total, C_NONE, -1, plain);
+        if (timing_on && log >= 0 && (e = timed(s, T_NONE, C_TRACE, log, plain)) != cudaSuccess) return e;
         float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
-        if ((e = wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
-                                     rb.idx.as<uint32_t>(), s)) != cudaSuccess)
+        if ((e = timed(s, total, C_MORTON, log, [&]() {
+                 return wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
+                                            rb.idx.as<uint32_t>(), s);
+             })) != cudaSuccess)
             return e;
-        if ((e = wfpt::launch_sort_pairs(rb.keys.p, rb.idx.as<uint32_t>(), n, n_dev, key_bits(), scratch.p,
-                                         scratch.bytes, s)) != cudaSuccess)
+        if ((e = timed(s, total, C_SORT, log, [&]() {
+                 return wfpt::launch_sort_pairs(rb.keys.p, rb.idx.as<uint32_t>(), n, n_dev, key_bits(), scratch.p,
+                                                scratch.bytes, s);
+             })) != cudaSuccess)
             return e;
         if (reorder) {
-            if ((e = wfpt::launch_reorder(rb.idx.as<uint32_t>(), rb.rays_cur(), rb.rays_out(), rb.s2i_cur(),
-                                          rb.s2i_out(), rb.i2s_out(), n, n_dev, s)) != cudaSuccess)
+            if ((e = timed(s, total, C_REORDER, log, [&]() {
+                     return wfpt::launch_reorder(rb.idx.as<uint32_t>(), rb.rays_cur(), rb.rays_out(), rb.s2i_cur(),
+                                                 rb.s2i_out(), rb.i2s_out(), n, n_dev, s);
+                 })) != cudaSuccess)
                 return e;
             rb.swap();
         }
-        return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
-                                  reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s, wk);
+        return timed(s, total, C_TRACE_SORT, log, [&]() {
+            return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(),
+                                      reorder ? nullptr : rb.idx.as<uint32_t>(), n, n_dev, closest ? 1 : 0, s, wk);
+        });
     }
 
     int primary_kind() const { return cfg.primary_bvh_kind >= 0 ? cfg.primary_bvh_kind : cfg.bvh_kind; }
@@ -359,13 +441,13 @@ struct wfpt_renderer {
     // order of the additions into out_pixels.
     cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
                             const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
-                            uint32_t* batch_counter, cudaStream_t s, int kind) {
+                            uint32_t* batch_counter, cudaStream_t s, int kind, int slot) {
         int S = cfg.num_shadow_samples;
         uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
         uint32_t bb = 0;
         cudaError_t e;
         if ((e = join_shadow(s)) != cudaSuccess) return e;
-        if (cfg.shadow_overlap && side && n_in <= batch_diff) {
+        if (cfg.shadow_overlap && side && n_in <= batch_diff && !timing_on) {
             const uint32_t* n_sh_dev = nullptr;
             if (n_in_dev) {
                 if ((e = wfpt::launch_batch_count(n_in_dev, 0, n_in, S, batch_counter, s)) != cudaSuccess) return e;
@@ -399,12 +481,14 @@ struct wfpt_renderer {
                 n_sh_dev = batch_counter;
             }
             shadow.swapped = false;
-            if ((e = wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, shadow.rays_cur(),
-                                                shadow.s2i_cur(), shadow.i2s_cur(), light, cfg.shadow_radius, (int)bb,
-                                                (int)bs, n_in_dev, S, s)) != cudaSuccess)
+            if ((e = timed(s, T_SHADOW, C_NONE, -1, [&]() {
+                     return wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, shadow.rays_cur(),
+                                                       shadow.s2i_cur(), shadow.i2s_cur(), light, cfg.shadow_radius,
+                                                       (int)bb, (int)bs, n_in_dev, S, s);
+                 })) != cudaSuccess)
                 return e;
             if ((e = trace_rays(shadow, bs * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
-                                cfg.reorder_shadow_rays != 0, false, s, false, kind)) != cudaSuccess)
+                                cfg.reorder_shadow_rays != 0, false, s, false, kind, T_SHADOW, slot)) != cudaSuccess)
                 return e;
             if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
                                                      in_pixels, out_pixels, (int)bb, (int)bs, n_in_dev, S, 0, s)) !=
@@ -421,12 +505,15 @@ struct wfpt_renderer {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
         int sample_index = pass + cfg.num_primary_samples * (frame_index - 1);
-        if ((e = wfpt::launch_raygen_primary(s2w, i2p.as<int32_t>(), primary.rays_cur(), eye, sample_index, width,
-                                             height, zfar, s, fp, pass, cfg.num_primary_samples)) != cudaSuccess)
-            return e;
-        if ((e = wfpt::launch_trace(*wfpt::scene_device(scene), primary_kind(), primary.rays_cur(),
-                                    primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s,
-                                    work.as<uint32_t>())) != cudaSuccess)
+        if ((e = timed(s, T_PRIMARY, C_NONE, -1, [&]() {
+                 cudaError_t r = wfpt::launch_raygen_primary(s2w, i2p.as<int32_t>(), primary.rays_cur(), eye,
+                                                             sample_index, width, height, zfar, s, fp, pass,
+                                                             cfg.num_primary_samples);
+                 if (r != cudaSuccess) return r;
+                 return wfpt::launch_trace(*wfpt::scene_device(scene), primary_kind(), primary.rays_cur(),
+                                           primary.results.as<wfpt_hit>(), nullptr, n, nullptr, 1, s,
+                                           work.as<uint32_t>());
+             })) != cudaSuccess)
             return e;
         const float one = 1.0f;
         uint32_t one_bits;
@@ -446,6 +533,8 @@ struct wfpt_renderer {
                       cudaStream_t s, const wfpt::FrameParams* fp = nullptr) {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
+        tev_used = 0;
+        spans.clear();
         primary.swapped = queue[0].swapped = queue[1].swapped = shadow.swapped = false;
         if ((e = cudaMemsetAsync(frame_pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(counters.p, 0, (size_t)cfg.num_primary_samples * kCountersPerPass * 4, s)) !=
@@ -469,7 +558,7 @@ struct wfpt_renderer {
             if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp)) != cudaSuccess) return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
                                  auxb[ai], frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s,
-                                 primary_kind())) != cudaSuccess)
+                                 primary_kind(), 0)) != cudaSuccess)
                 return e;
             if (rt != WFPT_PATH_RAYS) continue;
             int qsel = 0;  // PathQueue::swapBuffers
@@ -496,14 +585,15 @@ struct wfpt_renderer {
                 out.swapped = false;
                 uint32_t* out_cnt = cnt(pass, kCntPath + bounce);
                 // Renderer::pathPass -> tracePathRays (Renderer.cpp:156-162, 277-297).
-                if ((e = wfpt::launch_raygen_path(seeds.as<uint32_t>(), geoms, in_rays, out.rays_cur(), in_s2i,
-                                                  out.s2i_cur(), in_res, decreases.as<float>(), out_cnt, n, in_cnt,
-                                                  cfg.albedo, path_scratch.p, s)) != cudaSuccess)
+                if ((e = timed(s, T_PATH, C_NONE, -1, [&]() {
+                         return wfpt::launch_raygen_path(seeds.as<uint32_t>(), geoms, in_rays, out.rays_cur(), in_s2i,
+                                                         out.s2i_cur(), in_res, decreases.as<float>(), out_cnt, n,
+                                                         in_cnt, cfg.albedo, path_scratch.p, s);
+                     })) != cudaSuccess)
                     return e;
                 const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
                 if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s, false,
-                                    cfg.bvh_kind)) !=
-                    cudaSuccess)
+                                    cfg.bvh_kind, T_PATH, 100 + bounce)) != cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
                                                          auxb[ai], decreases.as<float>(), geoms, light, bg, n,
@@ -511,12 +601,15 @@ struct wfpt_renderer {
                     return e;
                 if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
                                      auxb[ai], frame_pixels, cnt(pass, kCntHits + bounce + 1),
-                                     cnt(pass, kCntBatch), s, cfg.bvh_kind)) != cudaSuccess)
+                                     cnt(pass, kCntBatch), s, cfg.bvh_kind, bounce + 1)) != cudaSuccess)
                     return e;
                 qsel ^= 1;  // PathQueue::swap
             }
         }
         if ((e = join_shadow(s)) != cudaSuccess) return e;
+        if (cfg.accumulate_fp64)
+            return wfpt::launch_interpolate_colors_fp64(frame_pixels, pixels, accum64.as<double>(), n, frame_index,
+                                                        cfg.key_value, cfg.white_point, s, fp);
         return wfpt::launch_interpolate_colors(frame_pixels, pixels, n, frame_index, cfg.key_value, cfg.white_point, s,
                                                fp);
     }
@@ -543,6 +636,8 @@ wfpt_status check_config(const wfpt_renderer_config* c) {
     if (c->shadow_overlap < 0 || c->shadow_overlap > 1) return WFPT_ERR_INVALID_ARGUMENT;
     if (c->primary_bvh_kind != -1 && c->primary_bvh_kind != WFPT_BVH2_FP32 && c->primary_bvh_kind != WFPT_BVH8_Q8)
         return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->timing < 0 || c->timing > 1) return WFPT_ERR_INVALID_ARGUMENT;
+    if (c->accumulate_fp64 < 0 || c->accumulate_fp64 > 1) return WFPT_ERR_INVALID_ARGUMENT;
     return WFPT_OK;
 }
 
@@ -574,6 +669,8 @@ void wfpt_renderer_config_default(wfpt_renderer_config* c) {
     c->path_sort_skip = 0;
     c->shadow_overlap = 1;
     c->primary_bvh_kind = -1;
+    c->timing = 0;
+    c->accumulate_fp64 = 0;
 }
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config, wfpt_renderer** renderer) {
@@ -659,10 +756,14 @@ wfpt_status wfpt_renderer_render(wfpt_renderer* r, const wfpt_camera* camera, in
         return WFPT_ERR_INVALID_ARGUMENT;
     }
     if ((e = cudaEventRecord(r->ev0, s)) != cudaSuccess) return wfpt::from_cuda(e);
-    if (r->cfg.use_graph)
+    r->timing_on = r->cfg.timing != 0;
+    r->last_timed = false;
+    if (r->cfg.use_graph && !r->timing_on)
         e = r->render_graph(s2w, camera->position, camera->zfar, pixels, frame_pixels, s);
     else
         e = r->frame(s2w, camera->position, camera->zfar, pixels, frame_pixels, s);
+    r->last_timed = r->timing_on && e == cudaSuccess;
+    r->timing_on = false;
     if (e != cudaSuccess) return wfpt::from_cuda(e);
     if ((e = cudaEventRecord(r->ev1, s)) != cudaSuccess) return wfpt::from_cuda(e);
     size_t cbytes = (size_t)r->cfg.num_primary_samples * kCountersPerPass * 4;
@@ -683,6 +784,7 @@ wfpt_status wfpt_renderer_get_stats(wfpt_renderer* r, wfpt_render_stats* st) {
     if (e != cudaSuccess) return wfpt::from_cuda(e);
     cudaEventElapsedTime(&r->frame_ms, r->ev0, r->ev1);
     r->fill_stats(st);
+    r->fill_times(st);
     st->frame_ms = r->frame_ms;
     return WFPT_OK;
 }

@@ -509,6 +509,39 @@ __global__ void k_interpolate_colors(float4* __restrict__ frame_pixels, float4* 
     }
 }
 
+// interpolateColors.comp:78-97 with the running mean kept in double: the
+// frame's colour (frame_pixels, float) is blended into accum (double4 per
+// pixel, w unused) with a = 1/frame and b = a * (frame - 1) in double, one
+// rounding per operation; pixels receives the mean rounded to float (w: the
+// frame colour's w on frame 1, 1 later, as the shader), and the tone map
+// (in float, as the shader) reads that rounding.
+__device__ __forceinline__ double dblend(double c1, double c0, double a, double b) {
+    return __dadd_rn(__dmul_rn(a, c1), __dmul_rn(b, c0));
+}
+
+__global__ void k_interpolate_colors_fp64(float4* __restrict__ frame_pixels, float4* __restrict__ pixels,
+                                          double4* __restrict__ accum, uint32_t n, int frame_index, float key,
+                                          float white, const FrameParams* __restrict__ fp) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (fp) frame_index = fp->frame_index;
+    float4 p1 = frame_pixels[i];
+    double4 m;
+    if (frame_index > 1) {
+        double4 m0 = accum[i];
+        double a = __ddiv_rn(1.0, (double)frame_index);
+        double b = __dmul_rn(a, __dsub_rn((double)frame_index, 1.0));
+        m = make_double4(dblend(p1.x, m0.x, a, b), dblend(p1.y, m0.y, a, b), dblend(p1.z, m0.z, a, b), 1.0);
+    } else {
+        m = make_double4(p1.x, p1.y, p1.z, 1.0);
+    }
+    accum[i] = m;
+    f3 c = mk(__double2float_rn(m.x), __double2float_rn(m.y), __double2float_rn(m.z));
+    pixels[i] = make_float4(c.x, c.y, c.z, frame_index > 1 ? 1.0f : p1.w);
+    f3 t = tonemap_reinhard(c, key, white);
+    frame_pixels[i] = make_float4(t.x, t.y, t.z, 1.0f);
+}
+
 // Device-side size of one shadow batch: S * clamp(n_in - begin, 0, size).
 __global__ void k_batch_count(const uint32_t* __restrict__ n_in_dev, uint32_t begin, uint32_t size, uint32_t S,
                               uint32_t* __restrict__ out) {
@@ -758,6 +791,18 @@ cudaError_t launch_interpolate_colors(float* frame_pixels, float* pixels, uint32
     k_interpolate_colors<<<grid_for(n), kBlock, 0, s>>>(reinterpret_cast<float4*>(frame_pixels),
                                                         reinterpret_cast<float4*>(pixels), n, frame_index,
                                                         key, white, fp);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interpolate_colors_fp64(float* frame_pixels, float* pixels, double* accum, uint32_t n,
+                                           int frame_index, float key, float white, cudaStream_t s,
+                                           const FrameParams* fp) {
+    if (n == 0) return cudaSuccess;
+    k_interpolate_colors_fp64<<<grid_for(n), kBlock, 0, s>>>(reinterpret_cast<float4*>(frame_pixels),
+                                                             reinterpret_cast<float4*>(pixels),
+                                                             reinterpret_cast<double4*>(accum), n, frame_index, key,
+                                                             white, fp);
     count_launch();
     return cudaGetLastError();
 }

@@ -64,6 +64,9 @@ cudaError_t launch_count_hits(const wfpt_hit* res, uint32_t n, const uint32_t* n
                               cudaStream_t s);
 cudaError_t launch_interpolate_colors(float* frame_pixels, float* pixels, uint32_t n, int frame_index,
                                       float key, float white, cudaStream_t s, const FrameParams* fp = nullptr);
+cudaError_t launch_interpolate_colors_fp64(float* frame_pixels, float* pixels, double* accum, uint32_t n,
+                                           int frame_index, float key, float white, cudaStream_t s,
+                                           const FrameParams* fp = nullptr);
 // Host-side one-time set-up that must not happen inside a stream capture
 // (function attributes, occupancy queries).
 cudaError_t sort_prepare();
