@@ -62,6 +62,9 @@ CITY = dict(
     light=(320.0, 300.0, 320.0), background=(0.529, 0.808, 0.98),
     renderer=dict(num_shadow_samples=2, shadow_radius=4.0),
 )
+# The reference arm renders every 4th pixel-table slot of the courtyard frame
+# per step (a quarter of its rays, spread over the whole image).
+REF_PIXEL_STRIDE = 4
 WORKLOAD_NAME = ("courtyard: 268,304 triangles, 1920x1080, 1 spp, path rays, 8 bounces, 2 shadow samples; "
                  "chosen form = BVH8-Q8 + persistent graph-captured wavefront + 64-bit 6-D Morton sort/reorder "
                  "of the path rays of every bounce")
@@ -72,6 +75,13 @@ METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s 
 # `bench.py --micro-only` (dram__bytes_read.sum + dram__bytes_write.sum,
 # cold caches): closest 87.6 MB + 10.2 MB, any-hit 152.9 MB + 40.6 MB.
 TRACE_DRAM_BYTES_PER_RAY = {"any": 46.64, "closest": 47.20}
+
+
+def workload_config(triangles, world):
+    """The `config` of the bench line, the same for both arms."""
+    return {"workload": WORKLOAD_NAME, "resolution": [COURTYARD["width"], COURTYARD["height"]],
+            "triangles": int(triangles), "parallelism": f"replicas x{world}",
+            "l2": "frame working set (>1 GB of ray/hit/key buffers) exceeds the 129 MB L2"}
 
 
 def peaks():
@@ -397,11 +407,9 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_c / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
-            "config": {"workload": WORKLOAD_NAME, "resolution": [w, h], "triangles": int(scene.info.num_triangles),
-                       "rays_per_frame": int(rays_per_frame),
-                       "path_rays_per_bounce": list(st_c.path_rays_per_bounce),
-                       "parallelism": f"replicas x{world}",
-                       "l2": "frame working set (>1 GB of ray/hit/key buffers) exceeds the 129 MB L2"},
+            "config": workload_config(scene.info.num_triangles, world),
+            "rays_per_frame": int(rays_per_frame),
+            "path_rays_per_bounce": list(st_c.path_rays_per_bounce),
             "plain": {"value": round(plain_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_p / args.steps, 4),
                       "rays_per_frame": int(st_p.num_primary_rays + st_p.num_shadow_rays + st_p.num_path_rays)},
             "chosen_over_plain": round(value / plain_value, 3),
@@ -672,12 +680,12 @@ def cpu_stages(wf, api, dev, scene, geom, cam, n_sample=1 << 20):
 
     (keys, ids), dt = timed(lambda: oracle.morton(p, smin, ssize, 2))
     out["morton_6d64"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "threads": th}
-    (_, order), dt = timed(lambda: oracle.sort_pairs(keys, ids, 63))
+    (_, order), dt = timed(lambda: oracle.sort_pairs_mt(keys, ids, 63))
     out["sort_u64_63bit"] = {"mpairs_s": round(p.shape[0] / dt / 1e6, 2), "gbs": round(192.0 * p.shape[0] / dt / 1e9, 3),
-                             "threads": 1}
+                             "threads": th, "method": "LSD radix, 8-bit digits, OpenMP"}
     _, dt = timed(lambda: oracle.reorder(order, p, np.arange(p.shape[0], dtype=np.int32)))
     out["reorder"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "gbs": round(80.0 * p.shape[0] / dt / 1e9, 3),
-                      "threads": 1}
+                      "threads": th}
     _, dt = timed(lambda: oracle.trace_bvh2(nodes, tris, p, closest=True))
     out["trace_closest"] = {"mrays_s": round(p.shape[0] / dt / 1e6, 2), "threads": th}
     _, dt = timed(lambda: oracle.trace_bvh2(nodes, tris, s, closest=False))
@@ -697,35 +705,57 @@ def cpu_baseline(args, wf, api, scene, pos, nrm, idx):
 
 # ---------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's stage chain
+    (oracle/, its restatement pinned to the reference's own sources) on the
+    host cores, with its own scene generation, BVH2 build and camera: the
+    process maps no product library.  The workload and `config` are the
+    repo arm's (the courtyard at 1920x1080, chosen-form settings); each
+    step renders a sample of that frame, every REF_PIXEL_STRIDE-th slot of
+    its pixel table (the same camera rays, spread over the whole image), so
+    that --steps 20 --warmup 5 ends within a few minutes."""
     world, rank, local = setup_dist()
     if rank != 0:
         return None
     import oracle
-    import vulkanwavefrontpathtracer_gb300 as wf
-    from vulkanwavefrontpathtracer_gb300 import build as wbuild
-    wbuild.build()
-    api = wf.api
     W = COURTYARD
-    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
-    scene = api.Scene(pos, idx, host_only=True)
-    w, h = 960, 540  # a quarter of the pixels per step keeps --steps 50 within a few minutes
+    pos, nrm, idx = oracle.generate_scene(W["scene_kind"], W["seed"])
+    nodes, tris = oracle.bvh2_build(pos, idx)
+    hg = oracle.HostGeometry(oracle.gltf_vertices(pos, nrm), idx)
+    w, h = W["width"], W["height"]
+    c = W["camera"]
+    s2w = oracle.camera_screen_to_world(c["position"], c["rotation_deg"], c["fov_deg"], w / h, c["znear"], c["zfar"])
+    R, F = W["renderer"], CHOSEN
+    cfg = oracle.FrameCfg(ray_type=2, spp=1, S=R["num_shadow_samples"], depth=R["recursion_depth"],
+                          radius=R["shadow_radius"], key=R["key_value"], white=R["white_point"], albedo=R["albedo"],
+                          sort_shadow=F["sort_shadow_rays"], reorder_shadow=F["reorder_shadow_rays"],
+                          sort_path=F["sort_path_rays"], reorder_path=F["reorder_path_rays"],
+                          morton_kind=F["morton_kind"], frame_index=1, pixel_stride=REF_PIXEL_STRIDE)
+    smin, smax = pos.min(0), pos.max(0)
+
+    def step():
+        t0 = time.perf_counter()
+        _, _, st = oracle.render_frame(nodes, tris, hg, smin, smax, W["light"], W["background"], s2w, c["position"],
+                                       c["zfar"], w, h, cfg)
+        return st.primary + st.shadow + st.path, time.perf_counter() - t0
+
     for _ in range(args.warmup):
-        cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
+        step()
     total_rays, total_t = 0, 0.0
     for _ in range(args.steps):
-        r, dt = cpu_frame(args, api, scene, pos, nrm, idx, w, h, CHOSEN)
+        r, dt = step()
         total_rays += r
         total_t += dt
     value = total_rays / total_t / 1e6
     out = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_t / args.steps * 1e3, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded scene)", "config": {"workload": WORKLOAD_NAME},
+           "data": "synthetic (seeded scene)", "config": workload_config(idx.shape[0], world),
            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": oracle.num_threads(),
                             "kind": "port",
-                            "sample": f"each step one {w}x{h} frame of the courtyard workload (1/4 of the "
-                                      "pixels) on the CPU restatement of the reference shaders (the reference's "
-                                      "Vulkan/rayQuery path is unavailable on this box)"},
+                            "sample": f"each step every {REF_PIXEL_STRIDE}th pixel-table slot of the {w}x{h} "
+                                      f"courtyard frame ({int(total_rays / args.steps)} rays), rendered by the CPU "
+                                      "restatement of the reference shaders (pinned to their sources) with its own "
+                                      "BVH2; the reference's Vulkan/rayQuery path is unavailable on this box"},
            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return out

@@ -23,7 +23,7 @@ class FrameCfg(C.Structure):
                 ("radius", C.c_float), ("key", C.c_float), ("white", C.c_float), ("albedo", C.c_float),
                 ("sort_shadow", C.c_int), ("reorder_shadow", C.c_int), ("sort_path", C.c_int),
                 ("reorder_path", C.c_int), ("morton_kind", C.c_int), ("frame_index", C.c_int),
-                ("path_sort_skip", C.c_int), ("accumulate_fp64", C.c_int)]
+                ("path_sort_skip", C.c_int), ("accumulate_fp64", C.c_int), ("pixel_stride", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -119,6 +119,51 @@ def sort_pairs(keys, vals, key_bits):
     vals = np.ascontiguousarray(vals, np.uint32).copy()
     _call(load().orc_sort_pairs, ptr(keys), ptr(vals), C.c_uint32(keys.shape[0]), C.c_int(key_bits))
     return keys, vals
+
+
+def sort_pairs_mt(keys, vals, key_bits):
+    """The same order as sort_pairs, by the multi-threaded LSD radix sort."""
+    keys = np.ascontiguousarray(keys).copy()
+    vals = np.ascontiguousarray(vals, np.uint32).copy()
+    _call(load().orc_sort_pairs_mt, ptr(keys), ptr(vals), C.c_uint32(keys.shape[0]), C.c_int(key_bits))
+    return keys, vals
+
+
+def bvh2_build(positions, indices):
+    """The oracle's own binned-SAH BVH2 (traversal format of trace_bvh2):
+    (nodes uint8 [m, 64], triangle records uint8 [t, 48])."""
+    pos = np.ascontiguousarray(positions, np.float32)
+    idx = np.ascontiguousarray(indices, np.uint32)
+    nt = idx.size // 3
+    nodes = np.zeros((2 * max(nt, 1), 64), np.uint8)
+    tris = np.zeros((nt, 48), np.uint8)
+    load().orc_bvh2_build.restype = C.c_uint32
+    m = _call(load().orc_bvh2_build, ptr(pos), ptr(idx), C.c_uint32(nt), ptr(nodes), ptr(tris))
+    return nodes[:m].copy(), tris
+
+
+def generate_scene(kind, seed, num_triangles=0):
+    """The benchmark workloads' seeded scenes (positions, normals, indices),
+    from the generator the product uses, without loading the product."""
+    nv, nt = C.c_uint32(0), C.c_uint32(0)
+    lib = load()
+    if not lib.orc_generate_scene(C.c_int(kind), C.c_uint64(seed), C.c_uint32(num_triangles), None, None,
+                                  C.byref(nv), None, C.byref(nt)):
+        raise ValueError("unknown scene kind")
+    pos = np.empty((nv.value, 3), np.float32)
+    nrm = np.empty((nv.value, 3), np.float32)
+    idx = np.empty((nt.value, 3), np.uint32)
+    _call(lib.orc_generate_scene, C.c_int(kind), C.c_uint64(seed), C.c_uint32(num_triangles), ptr(pos), ptr(nrm),
+          C.byref(nv), ptr(idx), C.byref(nt))
+    return pos, nrm, idx
+
+
+def gltf_vertices(positions, normals):
+    """96-byte vkglTF::Vertex records (pos.xyz, normal.xyz, then zeros)."""
+    v = np.zeros((positions.shape[0], 24), np.float32)
+    v[:, 0:3] = positions
+    v[:, 3:6] = normals
+    return v
 
 
 def reorder(idx, in_rays, in_s2i, index_space=None):

@@ -8,11 +8,12 @@
 // expression rounds exactly as written (GLSL shaders are written the same
 // way, one rounding per operation).
 //
-// Parity status: the reference's own shaders cannot run here (Vulkan +
-// VK_KHR_ray_query, no graphics stack) and its tests hold no golden vectors,
-// so this restatement is pinned by hand-derived known-answer vectors in
-// tests/golden/ (TEA, Morton bit layouts, Sobol, pixel table, Reinhard) and
-// by an FP64 traversal oracle, not by outputs of the reference itself.
+// Parity status: pinned to the reference's own sources.  The shaders of
+// every stage except the rayQuery traversal, the pixel-table loops and the
+// camera header compile for the CPU (oracle/ref_build.py -> oracle/_ref);
+// tests/test_oracle_ref_cpu.py and tests/golden/ref_vectors.npz hold this
+// restatement to their outputs.  The traversal is checked by the FP64
+// oracle below; the sort's definition is the stable order by key.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -195,9 +196,8 @@ static float halton(int i, int base) {
     return r;
 }
 
-extern "C" void orc_raygen_primary(const float m[16], const int32_t* i2p, ORay* rays, const float o[3], int sample_index, int w,
-                        int h, float max_dist) {
-    long long n = (long long)w * h;
+static void raygen_primary_n(const float m[16], const int32_t* i2p, ORay* rays, const float o[3], int sample_index,
+                             int w, int h, float max_dist, long long n) {
     for (long long task = 0; task < n; ++task) {
         int pixel = i2p[task];
         int sx = pixel % w, sy = pixel / w;
@@ -212,6 +212,11 @@ extern "C" void orc_raygen_primary(const float m[16], const int32_t* i2p, ORay* 
         V3 d = normalize3(world - org);
         rays[task] = ORay{o[0], o[1], o[2], 0.0f, d.x, d.y, d.z, max_dist};
     }
+}
+
+extern "C" void orc_raygen_primary(const float m[16], const int32_t* i2p, ORay* rays, const float o[3], int sample_index, int w,
+                        int h, float max_dist) {
+    raygen_primary_n(m, i2p, rays, o, sample_index, w, h, max_dist, (long long)w * h);
 }
 
 // ---------------------------------------------------------------- Morton
@@ -305,11 +310,77 @@ extern "C" void orc_sort_pairs(void* keys, uint32_t* vals, uint32_t n, int key_b
     }
 }
 
+// The same stable order by the masked key, by a parallel LSD radix sort with
+// 8-bit digits (per-thread digit counts over contiguous chunks, prefix over
+// (digit, thread), stable scatter): the multi-threaded CPU baseline of the
+// sort stage.  Equal to orc_sort_pairs on every input.
+template <class K>
+static void lsd_sort_mt(K* keys, uint32_t* vals, uint32_t n, int key_bits) {
+    std::vector<K> k2(n);
+    std::vector<uint32_t> v2(n);
+    K* ka = keys;
+    K* kb = k2.data();
+    uint32_t* va = vals;
+    uint32_t* vb = v2.data();
+    const int passes = (key_bits + 7) / 8;
+    int T = 1;
+#ifdef _OPENMP
+    T = std::max(1, omp_get_max_threads());
+#endif
+    std::vector<uint32_t> counts((size_t)T * 256);
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = 8 * pass;
+        const int bits = std::min(8, key_bits - shift);
+        const K mask = (K)((1u << bits) - 1u);
+        std::fill(counts.begin(), counts.end(), 0u);
+#pragma omp parallel num_threads(T)
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            uint64_t b = (uint64_t)n * t / T, e = (uint64_t)n * (t + 1) / T;
+            uint32_t* c = counts.data() + (size_t)t * 256;
+            for (uint64_t i = b; i < e; ++i) ++c[(uint32_t)((ka[i] >> shift) & mask)];
+#pragma omp barrier
+#pragma omp single
+            {
+                uint32_t run = 0;
+                for (int d = 0; d < 256; ++d)
+                    for (int tt = 0; tt < T; ++tt) {
+                        uint32_t x = counts[(size_t)tt * 256 + d];
+                        counts[(size_t)tt * 256 + d] = run;
+                        run += x;
+                    }
+            }
+            for (uint64_t i = b; i < e; ++i) {
+                uint32_t dst = c[(uint32_t)((ka[i] >> shift) & mask)]++;
+                kb[dst] = ka[i];
+                vb[dst] = va[i];
+            }
+        }
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    if (ka != keys) {
+        std::memcpy(keys, ka, (size_t)n * sizeof(K));
+        std::memcpy(vals, va, (size_t)n * 4);
+    }
+}
+
+extern "C" void orc_sort_pairs_mt(void* keys, uint32_t* vals, uint32_t n, int key_bits) {
+    if (key_bits <= 32)
+        lsd_sort_mt((uint32_t*)keys, vals, n, key_bits);
+    else
+        lsd_sort_mt((uint64_t*)keys, vals, n, key_bits);
+}
+
 // --------------------------------------------------------------- reorder
 // reorderRays.comp:37-45.
 extern "C" void orc_reorder(const uint32_t* idx, const ORay* in_rays, ORay* out_rays, const int32_t* in_s2i, int32_t* out_s2i,
                  int32_t* out_i2s, uint32_t n) {
-    for (uint32_t i = 0; i < n; ++i) {
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) {
         int32_t old = (int32_t)idx[i];
         int32_t index = in_s2i[old];
         out_rays[i] = in_rays[old];
@@ -790,6 +861,206 @@ extern "C" void orc_trace_bvh2(const void* nodes, const void* tris, const ORay* 
     }
 }
 
+// ----------------------------------------------------- BVH2 build (own)
+// A binned-SAH BVH2 in the traversal format above, independent of the
+// product's builder, so that a CPU run needs nothing of the product: 16
+// centroid bins per axis, leaves of at most 4 triangles (8 when the SAH
+// prefers or the centroids coincide), triangle records in leaf order.
+// Stored boxes are grown by 2^-22 * P (P: the largest absolute coordinate)
+// so that culling stays conservative for rays that start on a surface.
+namespace {
+struct BuildTri {
+    float lo[3], hi[3], c[3];
+};
+struct Bvh2Builder {
+    const float* pos;
+    const uint32_t* idx;
+    std::vector<BuildTri> bt;
+    std::vector<uint32_t> order;
+    std::vector<Node2> nodes;
+    float grow = 0.0f;
+
+    static float area(const float lo[3], const float hi[3]) {
+        float d[3] = {std::max(0.0f, hi[0] - lo[0]), std::max(0.0f, hi[1] - lo[1]), std::max(0.0f, hi[2] - lo[2])};
+        return d[0] * d[1] + d[1] * d[2] + d[2] * d[0];
+    }
+    void box(uint32_t b, uint32_t e, float lo[3], float hi[3], float clo[3], float chi[3]) const {
+        for (int k = 0; k < 3; ++k) lo[k] = clo[k] = FLT_MAX, hi[k] = chi[k] = -FLT_MAX;
+        for (uint32_t i = b; i < e; ++i) {
+            const BuildTri& t = bt[order[i]];
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], t.lo[k]);
+                hi[k] = std::max(hi[k], t.hi[k]);
+                clo[k] = std::min(clo[k], t.c[k]);
+                chi[k] = std::max(chi[k], t.c[k]);
+            }
+        }
+    }
+    int32_t leaf(uint32_t b, uint32_t e) const { return (int32_t)~((b << 3) | (e - b - 1)); }
+    // Builds order[b, e); returns its link and writes its (grown) box.  The
+    // root is always an inner node (traversal starts at node 0).
+    int32_t build(uint32_t b, uint32_t e, float out_lo[3], float out_hi[3], bool root = false) {
+        float lo[3], hi[3], clo[3], chi[3];
+        box(b, e, lo, hi, clo, chi);
+        for (int k = 0; k < 3; ++k) {
+            out_lo[k] = lo[k] - grow;
+            out_hi[k] = hi[k] + grow;
+        }
+        const uint32_t n = e - b;
+        if (n <= 4 && !root) return leaf(b, e);
+        const int NB = 16;
+        int best_axis = -1, best_split = 0;
+        float best_cost = FLT_MAX;
+        for (int ax = 0; ax < 3; ++ax) {
+            float ext = chi[ax] - clo[ax];
+            if (!(ext > 0.0f)) continue;
+            float blo[NB][3], bhi[NB][3];
+            uint32_t cnt[NB] = {0};
+            for (int i = 0; i < NB; ++i)
+                for (int k = 0; k < 3; ++k) blo[i][k] = FLT_MAX, bhi[i][k] = -FLT_MAX;
+            for (uint32_t i = b; i < e; ++i) {
+                const BuildTri& t = bt[order[i]];
+                int bin = std::min(NB - 1, (int)((t.c[ax] - clo[ax]) / ext * NB));
+                ++cnt[bin];
+                for (int k = 0; k < 3; ++k) {
+                    blo[bin][k] = std::min(blo[bin][k], t.lo[k]);
+                    bhi[bin][k] = std::max(bhi[bin][k], t.hi[k]);
+                }
+            }
+            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            float rarea[NB];
+            uint32_t rcnt[NB];
+            uint32_t run = 0;
+            for (int i = NB - 1; i > 0; --i) {
+                run += cnt[i];
+                for (int k = 0; k < 3; ++k) {
+                    rlo[k] = std::min(rlo[k], blo[i][k]);
+                    rhi[k] = std::max(rhi[k], bhi[i][k]);
+                }
+                rarea[i] = area(rlo, rhi);
+                rcnt[i] = run;
+            }
+            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            uint32_t lrun = 0;
+            for (int i = 0; i < NB - 1; ++i) {
+                lrun += cnt[i];
+                for (int k = 0; k < 3; ++k) {
+                    llo[k] = std::min(llo[k], blo[i][k]);
+                    lhi[k] = std::max(lhi[k], bhi[i][k]);
+                }
+                if (lrun == 0 || rcnt[i + 1] == 0) continue;
+                float cost = area(llo, lhi) * lrun + rarea[i + 1] * rcnt[i + 1];
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = ax;
+                    best_split = i + 1;
+                }
+            }
+        }
+        uint32_t m;
+        if (best_axis < 0) {
+            if (n <= 8 && !root) return leaf(b, e);
+            m = b + n / 2;  // coincident centroids: split by position in the list
+        } else {
+            // SAH with a node step and a triangle test of equal cost.
+            if (n <= 8 && !root && (float)n * area(lo, hi) <= area(lo, hi) + best_cost) return leaf(b, e);
+            float ext = chi[best_axis] - clo[best_axis];
+            auto mid = std::partition(order.begin() + b, order.begin() + e, [&](uint32_t t) {
+                int bin = std::min(NB - 1, (int)((bt[t].c[best_axis] - clo[best_axis]) / ext * NB));
+                return bin < best_split;
+            });
+            m = (uint32_t)(mid - order.begin());
+            if (m == b || m == e) m = b + n / 2;
+        }
+        if (n == 1) m = e;  // a one-triangle scene: both children are that leaf
+        int32_t id = (int32_t)nodes.size();
+        nodes.push_back(Node2{});
+        float l0[3], h0[3], l1[3], h1[3];
+        int32_t a = (m == e) ? leaf(b, e) : build(b, m, l0, h0);
+        int32_t c = (m == e) ? a : build(m, e, l1, h1);
+        if (m == e) {
+            for (int k = 0; k < 3; ++k) l0[k] = l1[k] = out_lo[k], h0[k] = h1[k] = out_hi[k];
+        }
+        Node2& nd = nodes[id];
+        nd.f[0] = l0[0]; nd.f[1] = h0[0]; nd.f[2] = l0[1]; nd.f[3] = h0[1];
+        nd.f[4] = l1[0]; nd.f[5] = h1[0]; nd.f[6] = l1[1]; nd.f[7] = h1[1];
+        nd.f[8] = l0[2]; nd.f[9] = h0[2]; nd.f[10] = l1[2]; nd.f[11] = h1[2];
+        nd.link[0] = a;
+        nd.link[1] = c;
+        nd.link[2] = nd.link[3] = 0;
+        return id;
+    }
+};
+}  // namespace
+
+// Builds the BVH2 of ntri triangles (one geometry: primitive id = global
+// index = triangle index).  nodes_out holds up to 2 * ntri nodes (64 bytes
+// each), tris_out ntri records (48 bytes); returns the node count.
+extern "C" uint32_t orc_bvh2_build(const float* pos, const uint32_t* idx, uint32_t ntri, void* nodes_out,
+                                   void* tris_out) {
+    Bvh2Builder B;
+    B.pos = pos;
+    B.idx = idx;
+    B.bt.resize(ntri);
+    B.order.resize(ntri);
+    float P = 0.0f;
+    for (uint32_t t = 0; t < ntri; ++t) {
+        BuildTri& x = B.bt[t];
+        for (int k = 0; k < 3; ++k) x.lo[k] = FLT_MAX, x.hi[k] = -FLT_MAX;
+        for (int v = 0; v < 3; ++v)
+            for (int k = 0; k < 3; ++k) {
+                float c = pos[3 * (size_t)idx[3 * (size_t)t + v] + k];
+                x.lo[k] = std::min(x.lo[k], c);
+                x.hi[k] = std::max(x.hi[k], c);
+                P = std::max(P, std::fabs(c));
+            }
+        for (int k = 0; k < 3; ++k) x.c[k] = 0.5f * (x.lo[k] + x.hi[k]);
+        B.order[t] = t;
+    }
+    B.grow = std::ldexp(P, -22);
+    B.nodes.reserve(2 * (size_t)ntri);
+    float lo[3], hi[3];
+    B.build(0, ntri, lo, hi, true);
+    std::memcpy(nodes_out, B.nodes.data(), B.nodes.size() * sizeof(Node2));
+    TriRec* T = (TriRec*)tris_out;
+    for (uint32_t i = 0; i < ntri; ++i) {
+        uint32_t t = B.order[i];
+        TriRec r;
+        for (int k = 0; k < 3; ++k) {
+            r.v0[k] = pos[3 * (size_t)idx[3 * (size_t)t + 0] + k];
+            r.v1[k] = pos[3 * (size_t)idx[3 * (size_t)t + 1] + k];
+            r.v2[k] = pos[3 * (size_t)idx[3 * (size_t)t + 2] + k];
+        }
+        r.prim = (int32_t)t;
+        r.geom = 0;
+        r.global = t;
+        T[i] = r;
+    }
+    return (uint32_t)B.nodes.size();
+}
+
+// The seeded synthetic scenes of the benchmark workloads, from the one
+// generator the product's wfpt_generate_scene also uses (compiled into this
+// library by oracle/build.py), so that a CPU run renders the same triangles
+// without loading the product library.  Two calls: sizes first (null
+// arrays), then the arrays.
+namespace wfpt {
+bool generate_scene(int kind, uint64_t seed, uint32_t ntri, std::vector<float>& pos, std::vector<float>& nrm,
+                    std::vector<uint32_t>& idx);
+}
+extern "C" int orc_generate_scene(int kind, uint64_t seed, uint32_t ntri, float* pos, float* nrm, uint32_t* nv,
+                                  uint32_t* idx, uint32_t* nt) {
+    std::vector<float> p, n;
+    std::vector<uint32_t> i;
+    if (!wfpt::generate_scene(kind, seed, ntri, p, n, i)) return 0;
+    *nv = (uint32_t)(p.size() / 3);
+    *nt = (uint32_t)(i.size() / 3);
+    if (pos) std::memcpy(pos, p.data(), p.size() * 4);
+    if (nrm) std::memcpy(nrm, n.data(), n.size() * 4);
+    if (idx) std::memcpy(idx, i.data(), i.size() * 4);
+    return 1;
+}
+
 // ------------------------------------------------- FP64 traversal oracle
 // Independent of the product's BVH: its own median-split BVH over FP64
 // triangle boxes and the watertight test evaluated in double.  Reports the
@@ -986,6 +1257,7 @@ struct OFrameCfg {
     int frame_index;
     int path_sort_skip;  // bit b: bounce b+1 traces its path rays unsorted
     int accumulate_fp64;  // the running mean in the caller's double buffer
+    int pixel_stride;     // > 1: a sample of the frame, every stride-th slot of the pixel table
 };
 
 struct OStats {
@@ -1008,10 +1280,10 @@ static void trace_sort(const Node2* N, const TriRec* T, std::vector<ORay>& rays,
     if (mk == 0) {
         std::vector<uint32_t> k32(n);
         orc_morton(rays.data(), n, smin, ssize, 0, k32.data(), idx.data());
-        orc_sort_pairs(k32.data(), idx.data(), n, 32);
+        orc_sort_pairs_mt(k32.data(), idx.data(), n, 32);
     } else {
         orc_morton(rays.data(), n, smin, ssize, mk, keys.data(), idx.data());
-        orc_sort_pairs(keys.data(), idx.data(), n, bits);
+        orc_sort_pairs_mt(keys.data(), idx.data(), n, bits);
     }
     if (reorder) {
         orc_reorder(idx.data(), rays.data(), rays_alt.data(), s2i.data(), s2i_alt.data(), i2s_alt.data(), n);
@@ -1030,16 +1302,24 @@ extern "C" void orc_render_frame(const void* nodes, const void* tris, const OGeo
                       double* accum) {
     const Node2* N = (const Node2*)nodes;
     const TriRec* T = (const TriRec*)tris;
-    uint32_t n = (uint32_t)w * (uint32_t)h;
+    const uint32_t npx = (uint32_t)w * (uint32_t)h;
     int S = cfg->S;
     float ssize[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
-    std::vector<int32_t> i2p(n), p2i(n);
+    std::vector<int32_t> i2p(npx), p2i(npx);
     orc_pixel_table(w, h, i2p.data(), p2i.data());
+    // The wavefront: every slot of the pixel table, or with pixel_stride > 1
+    // every stride-th one (a sample of the same frame's rays).
+    if (cfg->pixel_stride > 1) {
+        size_t k = 0;
+        for (size_t i = 0; i < npx; i += (size_t)cfg->pixel_stride) i2p[k++] = i2p[i];
+        i2p.resize(k);
+    }
+    const uint32_t n = (uint32_t)i2p.size();
     std::vector<uint32_t> seeds(n);
-    std::vector<float> aux(4 * (size_t)n), dec(4 * (size_t)n);
+    std::vector<float> aux(4 * (size_t)npx), dec(4 * (size_t)npx);
     std::memset(stats, 0, sizeof(*stats));
-    std::fill(frame_pixels, frame_pixels + 4 * (size_t)n, 0.0f);
-    if (cfg->frame_index == 1) std::fill(pixels, pixels + 4 * (size_t)n, 0.0f);
+    std::fill(frame_pixels, frame_pixels + 4 * (size_t)npx, 0.0f);
+    if (cfg->frame_index == 1) std::fill(pixels, pixels + 4 * (size_t)npx, 0.0f);
     if (cfg->ray_type != 0) orc_init_seeds(seeds.data(), n, cfg->frame_index);
     std::vector<ORay> prim_rays(n);
     std::vector<OHit> prim_res(n);
@@ -1072,7 +1352,7 @@ extern "C" void orc_render_frame(const void* nodes, const void* tris, const OGeo
         float* target = cfg->ray_type == 0 ? frame_pixels : aux.data();
         if (cfg->ray_type != 0) std::fill(aux.begin(), aux.end(), 0.0f);
         int sample_index = pass + cfg->spp * (cfg->frame_index - 1);
-        orc_raygen_primary(s2w, i2p.data(), prim_rays.data(), eye, sample_index, w, h, zfar);
+        raygen_primary_n(s2w, i2p.data(), prim_rays.data(), eye, sample_index, w, h, zfar, n);
         orc_trace_bvh2(N, T, prim_rays.data(), prim_res.data(), nullptr, n, 1);
         std::fill(dec.begin(), dec.end(), 1.0f);
         orc_reconstruct_smooth(prim_rays.data(), prim_res.data(), i2p.data(), target, dec.data(), geoms, light, bg, n,
@@ -1088,7 +1368,8 @@ extern "C" void orc_render_frame(const void* nodes, const void* tris, const OGeo
         for (int bounce = 0; bounce < cfg->depth; ++bounce) {
             std::fill(aux.begin(), aux.end(), 0.0f);
             std::vector<ORay> out(n), out_alt(n);
-            std::vector<int32_t> out_s2i(n), s2i_alt(n), i2s_alt(n);
+            // index_to_slot of the path rays is indexed by pixel (slot_to_index holds pixels)
+            std::vector<int32_t> out_s2i(n), s2i_alt(n), i2s_alt(npx);
             std::vector<OHit> out_res(n);
             uint32_t cnt = orc_raygen_path(seeds.data(), geoms, in_rays.data(), out.data(), in_s2i.data(),
                                            out_s2i.data(), in_res.data(), dec.data(), n_in, cfg->albedo);
@@ -1109,7 +1390,7 @@ extern "C" void orc_render_frame(const void* nodes, const void* tris, const OGeo
         }
     }
     if (cfg->accumulate_fp64)
-        orc_interpolate_colors_fp64(frame_pixels, pixels, accum, n, cfg->frame_index, cfg->key, cfg->white);
+        orc_interpolate_colors_fp64(frame_pixels, pixels, accum, npx, cfg->frame_index, cfg->key, cfg->white);
     else
-        orc_interpolate_colors(frame_pixels, pixels, n, cfg->frame_index, cfg->key, cfg->white);
+        orc_interpolate_colors(frame_pixels, pixels, npx, cfg->frame_index, cfg->key, cfg->white);
 }

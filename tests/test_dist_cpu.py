@@ -63,3 +63,34 @@ def test_reference_arm_runs_on_rank_zero_only():
                          env=_env(1, 2, port), capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, res.stderr
     assert res.stdout.strip() == ""
+
+
+REF_CHILD = r"""
+import json, sys, types
+sys.path.insert(0, sys.argv[1])
+import bench
+args = types.SimpleNamespace(steps=1, warmup=0, gpus=1)
+out = bench.run_reference(args)
+maps = open("/proc/self/maps").read()
+print(json.dumps({"line": out, "libwfpt": "libwfpt.so" in maps, "liboracle": "liboracle.so" in maps,
+                  "torch": "torch" in sys.modules and "libtorch" in maps}))
+"""
+
+
+def test_reference_arm_maps_no_product_library():
+    """The reference arm generates the scene, builds its BVH2 and renders
+    with the oracle alone: libwfpt.so is never loaded into its process, and
+    its config is the repo arm's workload config."""
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    res = subprocess.run([sys.executable, "-c", REF_CHILD, str(ROOT)], env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stderr
+    o = json.loads(res.stdout.strip().splitlines()[-1])
+    assert o["liboracle"] and not o["libwfpt"]
+    line = o["line"]
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert line["config"] == bench.workload_config(268304, 1)
+    assert line["impl"] == "reference" and line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
