@@ -152,6 +152,10 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          allocated); -1 (default) off
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
+ *   "renderer.shadow_slots"  shadow batches a renderer runs at once in an
+ *                          overlapped shadow pass: 0 (default) = planned
+ *                          from free device memory, 1..8 = that many
+ *                          (capped by the batches a pass can need)
  * Unknown keys and out-of-range values return WFPT_ERR_INVALID_ARGUMENT. */
 wfpt_status wfpt_tune_set(const char* key, int64_t value);
 wfpt_status wfpt_tune_get(const char* key, int64_t* value);
@@ -581,6 +585,12 @@ typedef struct wfpt_render_stats {
      * passes, ray counts for every pass. */
     wfpt_sort_log shadow_sort_logs[9];
     wfpt_sort_log path_sort_logs[8];
+    /* Shadow batches of the last frame that ran at once: the renderer's
+     * memory planner gives overlapped shadow passes up to
+     * min(batches, 8) slots, as many as fit in half of the free device
+     * memory (knob renderer.shadow_slots forces a count); 1 when the
+     * batches ran one after another. */
+    int shadow_batch_slots;
 } wfpt_render_stats;
 
 wfpt_status wfpt_renderer_create(const wfpt_renderer_config* config,

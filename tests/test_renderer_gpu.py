@@ -313,6 +313,53 @@ def test_multi_batch_shadow_frame_matches_oracle(wf, orc, dev, overlap):
                                    dict(bench.CHOSEN, shadow_overlap=overlap),
                                    cfg_over=dict(num_shadow_samples=9, recursion_depth=2))
     assert st.num_primary_rays * 9 > 8 * 1024 * 1024
+    # The memory planner runs the two batches on two slots when passes
+    # overlap (a GB300 has the memory for both).
+    assert st.shadow_batch_slots == (2 if overlap else 1)
+
+
+@pytest.mark.parametrize("slots,sort_shadow", [(1, 0), (2, 0), (0, 0), (2, 1)])
+def test_shadow_batch_slots_identical_frames(wf, dev, slots, sort_shadow):
+    """17 shadow samples at 1024x1024: the primary shadow pass is three
+    batches (493,447 + 493,447 + 61,682 inputs).  Run one after another on
+    the frame's stream, on 1 or 2 slots (the third batch reuses slot 0) or on
+    as many as the planner gives (3), with and without sorted shadow rays,
+    the frames and ray counts are the same bit for bit."""
+    import bench
+    import torch
+    W = bench.COURTYARD
+    pos, nrm, idx = wf.api.generate_scene(W["scene_kind"], W["seed"])
+    sc = wf.api.Scene(pos, idx)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    cam = wf.api.make_camera(**W["camera"])
+    w = h = 1024
+
+    def frame(overlap, knob):
+        old = wf.api.tune_get("renderer.shadow_slots")
+        try:
+            wf.api.tune_set("renderer.shadow_slots", knob)
+            r = wf.api.Renderer(**dict(bench.COURTYARD["renderer"], num_shadow_samples=17, recursion_depth=1,
+                                       bvh_kind=wf.BVH8_Q8, use_graph=1, shadow_overlap=overlap,
+                                       sort_shadow_rays=sort_shadow))
+            r.set_scene(sc, geom, W["light"], W["background"])
+            px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+            fp = torch.zeros_like(px)
+            for _ in range(2):  # graph replay of the captured frame, frame index 1 and 2
+                r.render(cam, w, h, px, fp)
+            st = r.stats()
+            out = (_canon_nan(N(px)).view(np.uint32), _canon_nan(N(fp)).view(np.uint32),
+                   (st.num_primary_rays, st.num_shadow_rays, st.num_path_rays), st.shadow_batch_slots)
+            r.close()
+            return out
+        finally:
+            wf.api.tune_set("renderer.shadow_slots", old)
+
+    ref = frame(0, 0)
+    got = frame(1, slots)
+    assert got[3] == (slots if slots else 3) and ref[3] == 1
+    assert got[2] == ref[2]
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert wf.api.device_status() == 0
 
 
 def test_fp64_accumulation_frames_match_oracle(wf, orc, dev, small):

@@ -111,6 +111,7 @@ class RenderStats(C.Structure):
         ("path_trace_ms", c_float),
         ("shadow_sort_logs", SortLog * 9),
         ("path_sort_logs", SortLog * 8),
+        ("shadow_batch_slots", c_int),
     ]
 
 

@@ -130,6 +130,11 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_fail_alloc_after((int)value);
         return WFPT_OK;
     }
+    if (k == "renderer.shadow_slots") {
+        if (value < 0 || value > 8) return invalid("renderer.shadow_slots must be 0 (planned) or in [1, 8]");
+        wfpt::set_shadow_slots((int)value);
+        return WFPT_OK;
+    }
     if (k == "build.ploc.radius") {
         if (value < 1 || value > 64) return invalid("build.ploc.radius must be in [1, 64]");
         wfpt::set_ploc_radius((int)value);
@@ -193,6 +198,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "debug.fail_alloc_after") {
         *value = wfpt::get_fail_alloc_after();
+        return WFPT_OK;
+    }
+    if (k == "renderer.shadow_slots") {
+        *value = wfpt::get_shadow_slots();
         return WFPT_OK;
     }
     if (k == "build.ploc.radius") {

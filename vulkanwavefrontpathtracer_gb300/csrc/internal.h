@@ -23,5 +23,8 @@ void scene_bounds(const wfpt_scene* s, float mn[3], float mx[3]);
 // Renderer allocation fault injection (renderer.cpp).
 void set_fail_alloc_after(int n);
 int get_fail_alloc_after();
+// Shadow batch slots of the renderer's memory planner (0 = planned).
+void set_shadow_slots(int n);
+int get_shadow_slots();
 
 }  // namespace wfpt

@@ -31,8 +31,15 @@ constexpr int kMaxSamples = 1024;               // RENDERER_MAX_SAMPLES
 constexpr int kMaxBatch = 8 * 1024 * 1024;      // RENDERER_MAX_BATCH_SIZE
 constexpr int kCountersPerPass = 32;
 // Per-pass counter block: [0..7] path rays per bounce, [8..16] hits among
-// the input rays of each shadow pass, [17] shadow rays of the current batch.
+// the input rays of each shadow pass, [17..24] shadow rays of the batch in
+// flight on each shadow slot.
 constexpr int kCntPath = 0, kCntHits = 8, kCntBatch = 17;
+
+// Shadow batch slots (knob "renderer.shadow_slots"): 0 = planned from free
+// device memory, 1..kMaxSlots = that many (capped by the batches a pass can
+// need).
+constexpr int kMaxSlots = 8;
+static std::atomic<int> g_shadow_slots{0};
 
 // Fault injection (knob "debug.fail_alloc_after"): when >= 0, the renderer's
 // allocation after that many more succeeds reports out of memory, without
@@ -114,14 +121,28 @@ struct wfpt_renderer {
     // one stream, one after another), so that renderers running
     // concurrently never share one.
     DevBuf work;
-    // Shadow-pass overlap (cfg.shadow_overlap): the shadow rays of a pass
-    // are traced and reconstructed on `side` while the next bounce runs on
-    // the frame's stream; that branch has its own work counters, sort
-    // scratch and colour buffer (aux2 alternates with aux per pass).
-    DevBuf aux2, work_side, sort_scratch_side;
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    bool shadow_pending = false;
+    // Shadow-pass overlap (cfg.shadow_overlap): the batches of a pass's
+    // shadow rays are generated, traced and reconstructed on the streams of
+    // `slots` (batch b on slot b % slots.size()) while the next bounce runs
+    // on the frame's stream; each slot has its own ray buffers, traversal
+    // work counters and sort scratch, and the colour buffers alternate
+    // between passes (aux2 with aux).  The batch boundaries are the
+    // reference's (RENDERER_MAX_BATCH_SIZE / S, Renderer.cpp:136-147): they
+    // decide which seed a shadow ray reads, so they stay fixed; the memory
+    // planner (prepare) only decides how many batches run at once.  The
+    // batches of one pass add into disjoint pixels, so running them
+    // concurrently gives the sequential result bit for bit.
+    struct ShadowSlot {
+        RayBufferDev rb;
+        DevBuf work, scratch;
+        cudaStream_t stream = nullptr;
+        cudaEvent_t ev_rg = nullptr, ev_done = nullptr;
+    };
+    std::vector<ShadowSlot> slots;
+    DevBuf aux2;
+    cudaEvent_t ev_fork = nullptr;
+    int pending_slots = 0;  // slots the next shadow pass (or the frame's end) waits for
+    int last_slots = 0;     // slots used by the last frame
     RayBufferDev primary, shadow, queue[2];
     DevBuf accum64;  // cfg.accumulate_fp64: the running mean, double4 per pixel
     uint32_t* host_counters = nullptr;  // pinned
@@ -172,6 +193,7 @@ struct wfpt_renderer {
         int w, h;
         const void *pixels, *frame_pixels, *scene, *geoms;
         float light[3], bg[3], smin[3], smax[3];
+        int slots;
     } graph_key{};
     bool graph_valid = false;
 
@@ -185,6 +207,7 @@ struct wfpt_renderer {
         k.frame_pixels = frame_pixels;
         k.scene = scene;
         k.geoms = geoms;
+        k.slots = nslots;
         for (int i = 0; i < 3; ++i) {
             k.light[i] = light[i];
             k.bg[i] = bg[i];
@@ -241,11 +264,16 @@ struct wfpt_renderer {
         if (graph) cudaGraphDestroy(graph);
         if (fp_dev) cudaFree(fp_dev);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        if (side) cudaStreamDestroy(side);
+        for (ShadowSlot& sl : slots) {
+            if (sl.stream) cudaStreamDestroy(sl.stream);
+            if (sl.ev_rg) cudaEventDestroy(sl.ev_rg);
+            if (sl.ev_done) cudaEventDestroy(sl.ev_done);
+            sl.rb.release();
+            sl.work.release();
+            sl.scratch.release();
+        }
         if (ev_fork) cudaEventDestroy(ev_fork);
-        if (ev_join) cudaEventDestroy(ev_join);
-        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters, &work, &aux2,
-                        &work_side, &sort_scratch_side})
+        for (auto* b : {&i2p, &p2i, &seeds, &decreases, &aux, &sort_scratch, &path_scratch, &counters, &work, &aux2})
             b->release();
         primary.release();
         shadow.release();
@@ -325,6 +353,30 @@ struct wfpt_renderer {
 
     uint32_t* cnt(int pass, int slot) const { return counters.as<uint32_t>() + pass * kCountersPerPass + slot; }
 
+    int nslots = 1;  // shadow batch slots of the current plan
+
+    // The memory planner's share for shadow batches: how many of a pass's
+    // batches (at most ceil(n / (kMaxBatch / S))) run at once.  Each slot
+    // holds one batch's rays (double-buffered), hits, slot maps, keys and
+    // sort scratch; the plan takes as many as fit in half of the device
+    // memory that is free before they are allocated (slots already held by
+    // this renderer count as free), at least one.
+    int plan_slots(size_t n, int S, size_t shadow_cap) const {
+        const size_t batch_diff = (size_t)(kMaxBatch / S);
+        const int batches = (int)std::min<size_t>(kMaxSlots, (n + batch_diff - 1) / batch_diff);
+        int want = g_shadow_slots.load() > 0 ? std::min(g_shadow_slots.load(), batches) : batches;
+        if (want <= 1) return 1;
+        const size_t per_slot = shadow_cap * (2 * 32 + 16 + 4 * 4 + 8 + 4) + 64 +
+                                (cfg.sort_shadow_rays ? wfpt::sort_scratch_bytes((uint32_t)shadow_cap, 64) : 0);
+        if (g_shadow_slots.load() > 0) return want;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1;
+        size_t held = 0;
+        for (const ShadowSlot& sl : slots) held += sl.rb.rays[0].bytes ? per_slot : 0;
+        const size_t budget = (free_b + held) / 2;
+        return (int)std::max<size_t>(1, std::min<size_t>((size_t)want, budget / per_slot));
+    }
+
     cudaError_t prepare(int w, int h) {
         cudaError_t e;
         size_t n = (size_t)w * h;
@@ -347,8 +399,9 @@ struct wfpt_renderer {
         if ((e = queue[1].ensure(n, true)) != cudaSuccess) return e;
         size_t batch_in = std::min<size_t>(n, (size_t)(kMaxBatch / S));
         size_t shadow_cap = std::max<size_t>(1, batch_in * S);
-        if ((e = shadow.ensure(shadow_cap, true)) != cudaSuccess) return e;
-        size_t sort_n = std::max(n, shadow_cap);
+        const bool sequential_shadow = !cfg.shadow_overlap || cfg.timing;
+        if (sequential_shadow && (e = shadow.ensure(shadow_cap, true)) != cudaSuccess) return e;
+        size_t sort_n = std::max(n, sequential_shadow ? shadow_cap : (size_t)0);
         if ((e = sort_scratch.ensure(wfpt::sort_scratch_bytes((uint32_t)sort_n, 64))) != cudaSuccess) return e;
         if ((e = path_scratch.ensure(wfpt::raygen_path_scratch_bytes((uint32_t)n))) != cudaSuccess) return e;
         if ((e = counters.ensure((size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess) return e;
@@ -359,16 +412,27 @@ struct wfpt_renderer {
         }
         if (cfg.shadow_overlap) {
             if ((e = aux2.ensure(n * 16)) != cudaSuccess) return e;
-            if (!work_side.p) {
-                if ((e = work_side.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
-                if ((e = cudaMemset(work_side.p, 0, work_side.bytes)) != cudaSuccess) return e;
-            }
-            if (cfg.sort_shadow_rays &&
-                (e = sort_scratch_side.ensure(wfpt::sort_scratch_bytes((uint32_t)shadow_cap, 64))) != cudaSuccess)
-                return e;
-            if (!side && (e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking)) != cudaSuccess) return e;
             if (!ev_fork && (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)) != cudaSuccess) return e;
-            if (!ev_join && (e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)) != cudaSuccess) return e;
+            const int want = plan_slots(n, S, shadow_cap);
+            if ((int)slots.size() < want) slots.resize(want);
+            for (int k = 0; k < want; ++k) {
+                ShadowSlot& sl = slots[k];
+                if ((e = sl.rb.ensure(shadow_cap, true)) != cudaSuccess) return e;
+                if (!sl.work.p) {
+                    if ((e = sl.work.ensure(16 * sizeof(uint32_t))) != cudaSuccess) return e;
+                    if ((e = cudaMemset(sl.work.p, 0, sl.work.bytes)) != cudaSuccess) return e;
+                }
+                if (cfg.sort_shadow_rays &&
+                    (e = sl.scratch.ensure(wfpt::sort_scratch_bytes((uint32_t)shadow_cap, 64))) != cudaSuccess)
+                    return e;
+                if (!sl.stream && (e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess)
+                    return e;
+                if (!sl.ev_rg && (e = cudaEventCreateWithFlags(&sl.ev_rg, cudaEventDisableTiming)) != cudaSuccess)
+                    return e;
+                if (!sl.ev_done && (e = cudaEventCreateWithFlags(&sl.ev_done, cudaEventDisableTiming)) != cudaSuccess)
+                    return e;
+            }
+            nslots = want;
         }
         if (!host_counters &&
             (e = cudaMallocHost(&host_counters, (size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess)
@@ -379,17 +443,16 @@ struct wfpt_renderer {
         return cudaSuccess;
     }
 
-    // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).  on_side: the
-    // launch belongs to the shadow branch (its own counters and scratch).
-    // total / log: where a timed frame books the stages (T_SHADOW or T_PATH;
+    // Tracer::trace / Tracer::traceSort (Tracer.cpp:185-225).  wk / scratch:
+    // the traversal work counters and sort scratch of the stream s (each
+    // concurrently running branch has its own).  total / log: where a timed frame books the stages (T_SHADOW or T_PATH;
     // the sort log slot); a timed sorted pass first traces its rays
     // unsorted, for the log's trace time, as Renderer.cpp:259-264 and
     // :281-286 do (the sorted trace then overwrites those results).
     cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
-                           cudaStream_t s, bool on_side, int kind, int total = T_NONE, int log = -1) {
+                           cudaStream_t s, uint32_t* wk, DevBuf& scratch, int kind, int total = T_NONE,
+                           int log = -1) {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
-        uint32_t* wk = on_side ? work_side.as<uint32_t>() : work.as<uint32_t>();
-        DevBuf& scratch = on_side ? sort_scratch_side : sort_scratch;
         cudaError_t e;
         auto plain = [&]() {
             return wfpt::launch_trace(sc, kind, rb.rays_cur(), rb.results.as<wfpt_hit>(), nullptr, n, n_dev,
@@ -424,61 +487,81 @@ struct wfpt_renderer {
 
     int primary_kind() const { return cfg.primary_bvh_kind >= 0 ? cfg.primary_bvh_kind : cfg.bvh_kind; }
 
-    // Makes stream s wait for the shadow branch forked last (if any).
+    // Makes stream s wait for the shadow batches forked last (if any).
     cudaError_t join_shadow(cudaStream_t s) {
-        if (!shadow_pending) return cudaSuccess;
-        shadow_pending = false;
-        return cudaStreamWaitEvent(s, ev_join, 0);
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < pending_slots && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(s, slots[k].ev_done, 0);
+        pending_slots = 0;
+        return e;
     }
 
     // Renderer::shadowPass (Renderer.cpp:133-154) over input rays `in`
     // whose slot->pixel map is `in_s2i`; n_in is the capacity, n_in_dev the
-    // device-side count (null when the host count is exact).  With
-    // shadow_overlap and a single batch, the shadow rays are generated on s
-    // (raygenShadow reads the seeds that the next raygenPath rewrites) and
-    // traced, reconstructed and counted on the side stream; join_shadow()
-    // waits for that branch before the next shadow pass, which keeps the
-    // order of the additions into out_pixels.
+    // device-side count (null when the host count is exact).  Batches of
+    // batch_diff input rays, as the reference cuts them.
+    //  - Overlapped (cfg.shadow_overlap, not timed): batch b is generated,
+    //    traced and reconstructed on the stream of slot b % nslots, forked
+    //    from s; s waits for the last batch generated on every slot before it
+    //    goes on (raygenShadow reads the seeds that the next raygenPath
+    //    rewrites), and join_shadow() makes the next shadow pass wait for
+    //    all of them, which keeps the order of the additions into
+    //    out_pixels.  A slot's batches run in order on its stream, so a
+    //    slot's buffers are reused only after its previous batch is done.
+    //  - Sequential: every batch on s, in the reference's order.
     cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
                             const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
-                            uint32_t* batch_counter, cudaStream_t s, int kind, int slot) {
-        int S = cfg.num_shadow_samples;
-        uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
-        uint32_t bb = 0;
+                            uint32_t* batch_counters, cudaStream_t s, int kind, int slot_log) {
+        const int S = cfg.num_shadow_samples;
+        const uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
         cudaError_t e;
         if ((e = join_shadow(s)) != cudaSuccess) return e;
-        if (cfg.shadow_overlap && side && n_in <= batch_diff && !timing_on) {
-            const uint32_t* n_sh_dev = nullptr;
-            if (n_in_dev) {
-                if ((e = wfpt::launch_batch_count(n_in_dev, 0, n_in, S, batch_counter, s)) != cudaSuccess) return e;
-                n_sh_dev = batch_counter;
-            }
-            shadow.swapped = false;
-            if ((e = wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, shadow.rays_cur(),
-                                                shadow.s2i_cur(), shadow.i2s_cur(), light, cfg.shadow_radius, 0,
-                                                (int)n_in, n_in_dev, S, s)) != cudaSuccess)
-                return e;
+        if (cfg.shadow_overlap && !timing_on && nslots >= 1 && (int)slots.size() >= nslots) {
             if ((e = cudaEventRecord(ev_fork, s)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
-            if ((e = trace_rays(shadow, n_in * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
-                                cfg.reorder_shadow_rays != 0, false, side, true, kind)) != cudaSuccess)
-                return e;
-            if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
-                                                     in_pixels, out_pixels, 0, (int)n_in, n_in_dev, S, 0, side)) !=
-                cudaSuccess)
-                return e;
-            if ((e = wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, side)) != cudaSuccess) return e;
-            if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
-            shadow_pending = true;
-            return cudaSuccess;
+            const uint32_t nb = (n_in + batch_diff - 1) / batch_diff;
+            const int used = (int)std::min<uint32_t>((uint32_t)nslots, std::max(nb, 1u));
+            for (int k = 0; k < used; ++k)
+                if ((e = cudaStreamWaitEvent(slots[k].stream, ev_fork, 0)) != cudaSuccess) return e;
+            for (uint32_t b = 0; b < nb; ++b) {
+                ShadowSlot& sl = slots[b % used];
+                const cudaStream_t ss = sl.stream;
+                const uint32_t bb = b * batch_diff, bs = std::min(batch_diff, n_in - bb);
+                const uint32_t* n_sh_dev = nullptr;
+                if (n_in_dev) {
+                    uint32_t* bc = batch_counters + (b % used);
+                    if ((e = wfpt::launch_batch_count(n_in_dev, bb, bs, S, bc, ss)) != cudaSuccess) return e;
+                    n_sh_dev = bc;
+                }
+                sl.rb.swapped = false;
+                if ((e = wfpt::launch_raygen_shadow(seeds.as<uint32_t>(), in_rays, in_res, sl.rb.rays_cur(),
+                                                    sl.rb.s2i_cur(), sl.rb.i2s_cur(), light, cfg.shadow_radius,
+                                                    (int)bb, (int)bs, n_in_dev, S, ss)) != cudaSuccess)
+                    return e;
+                if ((e = cudaEventRecord(sl.ev_rg, ss)) != cudaSuccess) return e;
+                if ((e = trace_rays(sl.rb, bs * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
+                                    cfg.reorder_shadow_rays != 0, false, ss, sl.work.as<uint32_t>(), sl.scratch,
+                                    kind)) != cudaSuccess)
+                    return e;
+                if ((e = wfpt::launch_reconstruct_shadow(sl.rb.results.as<wfpt_hit>(), in_s2i, sl.rb.i2s_cur(),
+                                                         in_pixels, out_pixels, (int)bb, (int)bs, n_in_dev, S, 0,
+                                                         ss)) != cudaSuccess)
+                    return e;
+            }
+            for (int k = 0; k < used; ++k) {
+                if ((e = cudaEventRecord(slots[k].ev_done, slots[k].stream)) != cudaSuccess) return e;
+                if ((e = cudaStreamWaitEvent(s, slots[k].ev_rg, 0)) != cudaSuccess) return e;
+            }
+            pending_slots = used;
+            last_slots = std::max(last_slots, used);
+            return wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, s);
         }
+        uint32_t bb = 0;
         do {
             uint32_t be = std::min(bb + batch_diff, n_in);
             uint32_t bs = be - bb;
             const uint32_t* n_sh_dev = nullptr;
             if (n_in_dev) {
-                if ((e = wfpt::launch_batch_count(n_in_dev, bb, bs, S, batch_counter, s)) != cudaSuccess) return e;
-                n_sh_dev = batch_counter;
+                if ((e = wfpt::launch_batch_count(n_in_dev, bb, bs, S, batch_counters, s)) != cudaSuccess) return e;
+                n_sh_dev = batch_counters;
             }
             shadow.swapped = false;
             if ((e = timed(s, T_SHADOW, C_NONE, -1, [&]() {
@@ -488,7 +571,8 @@ struct wfpt_renderer {
                  })) != cudaSuccess)
                 return e;
             if ((e = trace_rays(shadow, bs * (uint32_t)S, n_sh_dev, cfg.sort_shadow_rays != 0,
-                                cfg.reorder_shadow_rays != 0, false, s, false, kind, T_SHADOW, slot)) != cudaSuccess)
+                                cfg.reorder_shadow_rays != 0, false, s, work.as<uint32_t>(), sort_scratch, kind,
+                                T_SHADOW, slot_log)) != cudaSuccess)
                 return e;
             if ((e = wfpt::launch_reconstruct_shadow(shadow.results.as<wfpt_hit>(), in_s2i, shadow.i2s_cur(),
                                                      in_pixels, out_pixels, (int)bb, (int)bs, n_in_dev, S, 0, s)) !=
@@ -496,6 +580,7 @@ struct wfpt_renderer {
                 return e;
             bb = be;
         } while (bb != n_in);
+        last_slots = std::max(last_slots, 1);
         return wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, s);
     }
 
@@ -535,6 +620,7 @@ struct wfpt_renderer {
         cudaError_t e;
         tev_used = 0;
         spans.clear();
+        last_slots = 0;
         primary.swapped = queue[0].swapped = queue[1].swapped = shadow.swapped = false;
         if ((e = cudaMemsetAsync(frame_pixels, 0, (size_t)n * 16, s)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(counters.p, 0, (size_t)cfg.num_primary_samples * kCountersPerPass * 4, s)) !=
@@ -592,8 +678,9 @@ struct wfpt_renderer {
                      })) != cudaSuccess)
                     return e;
                 const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
-                if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s, false,
-                                    cfg.bvh_kind, T_PATH, 100 + bounce)) != cudaSuccess)
+                if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s,
+                                    work.as<uint32_t>(), sort_scratch, cfg.bvh_kind, T_PATH, 100 + bounce)) !=
+                    cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
                                                          auxb[ai], decreases.as<float>(), geoms, light, bg, n,
@@ -618,6 +705,8 @@ struct wfpt_renderer {
 namespace wfpt {
 void set_fail_alloc_after(int n) { g_fail_alloc_after = n < 0 ? -1 : n; }
 int get_fail_alloc_after() { return g_fail_alloc_after; }
+void set_shadow_slots(int n) { g_shadow_slots = n < 0 ? 0 : (n > kMaxSlots ? kMaxSlots : n); }
+int get_shadow_slots() { return g_shadow_slots; }
 }  // namespace wfpt
 
 namespace {
@@ -786,6 +875,7 @@ wfpt_status wfpt_renderer_get_stats(wfpt_renderer* r, wfpt_render_stats* st) {
     r->fill_stats(st);
     r->fill_times(st);
     st->frame_ms = r->frame_ms;
+    st->shadow_batch_slots = r->last_slots;
     return WFPT_OK;
 }
 
