@@ -75,6 +75,14 @@ METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s 
 # `bench.py --micro-only` (dram__bytes_read.sum + dram__bytes_write.sum,
 # cold caches): closest 87.6 MB + 10.2 MB, any-hit 152.9 MB + 40.6 MB.
 TRACE_DRAM_BYTES_PER_RAY = {"any": 46.64, "closest": 47.20}
+# Warp instructions per ray of the courtyard's bounce-1 BVH8 traversal
+# (sm__inst_executed.sum / rays of one launch each, `bench.py --trace-profile`
+# under ncu at 960x540: 284,186,300 for 518,400 sorted closest-hit path rays,
+# 338,336,587 for 1,036,800 any-hit shadow rays).  With the live launch time
+# they give the issue rate; the issue peak is 152 SMs x 4 schedulers x one
+# warp instruction per clock at the sampled SM clock.
+TRACE_WARP_INST_PER_RAY = {"any": 326.33, "closest": 548.20}
+NUM_SMS = 152
 
 
 def workload_config(triangles, world):
@@ -227,12 +235,13 @@ def city_frames(wf, api, dev, stream, scene, geom, steps=3):
                               "ms": round(e["ms"], 3)} for e in ktune["table"]]}}
 
 
-def city_bounce(wf, api, dev, stream, frames=True):
+def city_bounce(wf, api, dev, stream, frames=True, size=None):
     """The bounce-1 comparison of `bounce_micro` on the city block at
-    3840x2160 (8.3M primary rays) and, with `frames`, whole city frames
-    (city_frames).  Returns the per-bounce line (with the frames under
-    "frames") and the host-built city scene (for the build-time report)."""
-    W = CITY
+    3840x2160 (8.3M primary rays; `size` = (w, h) for a smaller profiling
+    case) and, with `frames`, whole city frames (city_frames).  Returns the
+    per-bounce line (with the frames under "frames") and the host-built city
+    scene (for the build-time report)."""
+    W = dict(CITY, width=size[0], height=size[1]) if size else CITY
     pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
     scene = api.Scene(pos, idx)
     geom = api.Geometry(pos, nrm, idx, device=dev)
@@ -395,10 +404,22 @@ def run_ours(args):
                     "note": "the BVH and triangles stay in L2, so DRAM carries only the ray and hit records; "
                             "the kernel is bound by instruction issue, not by HBM"}
 
+        def issue_roof(tr, kind):
+            mhz = clocks.summary().get("sm_mhz") or clocks.summary().get("sm_max_mhz") or 2070.0
+            peak_g = NUM_SMS * 4 * mhz * 1e6 / 1e9
+            ach_g = TRACE_WARP_INST_PER_RAY[kind] * tr["rays"] / (tr["ms"] * 1e-3) / 1e9
+            return {"bound": "issue", "achieved": round(ach_g, 1), "peak": round(peak_g, 1),
+                    "unit": "G warp instructions/s", "frac": round(ach_g / peak_g, 3),
+                    "warp_inst_per_ray": TRACE_WARP_INST_PER_RAY[kind], "sm_mhz": mhz,
+                    "source": "warp instructions per ray from one ncu launch of the same traversal at 960x540 "
+                              "(sm__inst_executed.sum); launch time measured here"}
+
         roof = trace_roof(micro["trace_shadow"], "k_trace_bvh8_coop<any-hit> (bounce-1 shadow rays, 2 per path ray)",
                           "any")
+        roof["issue_roofline"] = issue_roof(micro["trace_shadow"], "any")
         closest_roof = trace_roof(micro["trace_chosen"],
                                   "k_trace_bvh8_coop<closest> (bounce-1 path rays after sort+reorder)", "closest")
+        closest_roof["issue_roofline"] = issue_roof(micro["trace_chosen"], "closest")
         srt = micro["sort"]
         sort_roof = {"kernel": "radix sort u64 keys (63 bits, 8 passes) + u32 values", "bound": "hbm",
                      "achieved": srt["gbs"], "peak": hbm, "unit": "GB/s", "frac": srt["gbs"] / hbm,
@@ -567,6 +588,59 @@ def make_wavefronts(wf, api, dev, scene, geom, cam, w, h, light, shadow_samples=
     return path[:m].contiguous(), srays
 
 
+def run_trace_profile(args):
+    """A small case for kernel profiles: the bounce-1 path rays of the
+    courtyard (or, with --city, the city block) at --width x --height
+    (default 960x540) and the shadow rays of the bounce's hits (2 per path
+    ray, toward the light), each traversal form launched once after the
+    primary trace: BVH2 closest (unsorted), BVH8 closest (unsorted), BVH8
+    closest (6-D Morton sorted and reordered), BVH8 any hit, BVH2 any hit.
+    Prints the ray counts; the timings of these single launches are not
+    benchmark numbers."""
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    dev = torch.device("cuda", 0)
+    api = wf.api
+    W = CITY if args.city else COURTYARD
+    w, h = args.width or 960, args.height or 540
+    pos, nrm, idx = api.generate_scene(W["scene_kind"], W["seed"])
+    scene = api.Scene(pos, idx)
+    geom = api.Geometry(pos, nrm, idx, device=dev)
+    cam = api.make_camera(**W["camera"])
+    path, _ = make_wavefronts(wf, api, dev, scene, geom, cam, w, h, W["light"])
+    m = path.shape[0]
+    res = torch.empty((m, 4), dtype=torch.int32, device=dev)
+    keys = torch.empty(m, dtype=torch.int64, device=dev)
+    ids = torch.empty(m, dtype=torch.int32, device=dev)
+    api.morton(path, scene.bounds_min, scene.bounds_max - scene.bounds_min, wf.MORTON_6D64, keys, ids)
+    api.sort_pairs(keys, ids, 63)
+    srt = torch.empty_like(path)
+    api.reorder(ids, path, srt, torch.arange(m, dtype=torch.int32, device=dev),
+                torch.empty(m, dtype=torch.int32, device=dev), torch.empty(m, dtype=torch.int32, device=dev))
+    S = W["renderer"]["num_shadow_samples"]
+    seeds = torch.zeros(m, dtype=torch.int32, device=dev)
+    api.trace(scene, wf.BVH8_Q8, srt, res)
+    srays = torch.empty((S * m, 8), dtype=torch.float32, device=dev)
+    ss2i = torch.empty(S * m, dtype=torch.int32, device=dev)
+    si2s = torch.empty(S * m, dtype=torch.int32, device=dev)
+    api.raygen_shadow(seeds, srt, res, srays, ss2i, si2s, W["light"], W["renderer"]["shadow_radius"], 0, m, S)
+    sres = torch.empty((S * m, 4), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    # The profiled launches, in this order (after the primary trace and the
+    # sorted trace that made the shadow rays).
+    api.trace(scene, wf.BVH2_FP32, path, res)
+    api.trace(scene, wf.BVH8_Q8, path, res)
+    api.trace(scene, wf.BVH8_Q8, srt, res)
+    api.trace(scene, wf.BVH8_Q8, srays, sres, closest_hit=False)
+    api.trace(scene, wf.BVH2_FP32, srays, sres, closest_hit=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"trace_profile": "city" if args.city else "courtyard", "resolution": [w, h],
+                      "path_rays": m, "shadow_rays": S * m}))
+
+
 def run_sweep(args):
     """Autotuner searches on the courtyard wavefronts (prints one JSON line)."""
     import torch
@@ -582,6 +656,7 @@ def run_sweep(args):
     scene = api.Scene(pos, idx)
     geom = api.Geometry(pos, nrm, idx, device=dev)
     cam = api.make_camera(**W["camera"])
+    args.width, args.height = args.width or W["width"], args.height or W["height"]
     path, shadow = make_wavefronts(wf, api, dev, scene, geom, cam, args.width, args.height, W["light"])
     keys = autotune.tune_keys(scene, path)
     best = keys["best"]
@@ -623,8 +698,9 @@ def run_micro_only(args):
     wbuild.build()
     dev = torch.device("cuda", 0)
     api = wf.api
+    size = (args.width, args.height) if args.width and args.height else None
     if args.city:
-        line, _ = city_bounce(wf, api, dev, torch.cuda.current_stream(), frames=not args.no_city_frames)
+        line, _ = city_bounce(wf, api, dev, torch.cuda.current_stream(), frames=not args.no_city_frames, size=size)
         print(json.dumps({"per_bounce_city": line}))
         return
     W = COURTYARD
@@ -632,9 +708,10 @@ def run_micro_only(args):
     scene = api.Scene(pos, idx)
     geom = api.Geometry(pos, nrm, idx, device=dev)
     cam = api.make_camera(**W["camera"])
-    micro = bounce_micro(wf, api, dev, scene, geom, cam, args.width, args.height, torch.cuda.current_stream())
+    w, h = size or (W["width"], W["height"])
+    micro = bounce_micro(wf, api, dev, scene, geom, cam, w, h, torch.cuda.current_stream())
     print(json.dumps({"micro": micro["per_bounce"], "sort_gbs": round(micro["sort"]["gbs"], 1),
-                      "reorder_gbs": round(micro["reorder"]["gbs"], 1), "resolution": [args.width, args.height]}))
+                      "reorder_gbs": round(micro["reorder"]["gbs"], 1), "resolution": [w, h]}))
 
 
 # ---------------------------------------------------------- CPU baseline
@@ -972,18 +1049,23 @@ def main():
     ap.add_argument("--city", action="store_true",
                     help="with --micro-only: the bounce-1 comparison and whole frames on the city block at 3840x2160")
     ap.add_argument("--no-city-frames", action="store_true", help="with --city: the bounce-1 comparison only")
-    ap.add_argument("--width", type=int, default=COURTYARD["width"])
-    ap.add_argument("--height", type=int, default=COURTYARD["height"])
+    ap.add_argument("--width", type=int, default=None, help="with --micro-only: resolution of the bounce")
+    ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--sweep", action="store_true", help="run the autotuner searches and print their tables")
     ap.add_argument("--sort-micro", action="store_true", help="sort/reorder microbenchmark over --sort-sizes")
     ap.add_argument("--sort-sizes", default="65536,262144,1048576,2073600,4194304,16777216,67108864")
     ap.add_argument("--scene-build", action="store_true",
                     help="acceleration-structure build times only (host vs device; courtyard and city)")
     ap.add_argument("--batched", action="store_true", help="the 64-request batched serving workload")
+    ap.add_argument("--trace-profile", action="store_true",
+                    help="each traversal form launched once on a small bounce-1 case (for kernel profiles)")
     ap.add_argument("--batch-requests", type=int, default=64)
     args = ap.parse_args()
     if args.batched:
         run_batched(args)
+        return
+    if args.trace_profile:
+        run_trace_profile(args)
         return
     if args.scene_build:
         import torch
