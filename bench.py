@@ -386,10 +386,14 @@ def run_ours(args):
     hbm, peak_kind = peaks()
     out = None
     builds = city_line = None
+    sort_big = batched = None
     if rank == 0:
         city_line, city = city_bounce(wf, api, dev, stream)
         builds = scene_build_times(api, pos, idx, scene, city=city)
         del city
+        torch.cuda.empty_cache()
+        sort_big = sort_row(api, dev, stream)
+        batched = batched_serving(api, dev, stream, steps=3, warmup=1)
     if rank == 0:
         cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
         if cpu is not None:
@@ -447,6 +451,8 @@ def run_ours(args):
                                   "picked live on whole frames"},
             "per_bounce": micro["per_bounce"],
             "per_bounce_city": city_line,
+            "sort_2p26": sort_big,
+            "batched": batched,
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),
                              "reorder_frac": round(micro["reorder"]["gbs"] / hbm, 3)},
@@ -867,23 +873,16 @@ def batch_requests(seed=7, count=64):
     return out
 
 
-def run_batched(args):
-    """One step = one frame of all 64 requests: batched (one graph replay,
-    4 branches) against the same requests rendered one after another
+def batched_serving(api, dev, stream, count=64, steps=10, warmup=3):
+    """One step = one frame of all `count` requests: batched (one graph
+    replay, 4 branches) against the same requests rendered one after another
     through standalone renderers with every stage launched directly."""
     import torch
-
-    import vulkanwavefrontpathtracer_gb300 as wf
-    from vulkanwavefrontpathtracer_gb300 import build as wbuild
-    wbuild.build()
-    api = wf.api
-    dev = torch.device("cuda", 0)
-    stream = torch.cuda.current_stream()
     scenes = []
     for s in BATCH_SCENES:
         pos, nrm, idx = api.generate_scene(s["kind"], s["seed"], s["ntris"])
         scenes.append((api.Scene(pos, idx), api.Geometry(pos, nrm, idx, device=dev), int(idx.shape[0])))
-    specs = batch_requests(count=args.batch_requests)
+    specs = batch_requests(count=count)
     reqs, solos = [], []
     for q in specs:
         s = BATCH_SCENES[q["scene"]]
@@ -917,18 +916,72 @@ def run_batched(args):
         for r, cam, w, h, px, fp in solos:
             r.render(cam, w, h, px, fp)
 
-    ms_batch = timed(batch.render, args.steps, args.warmup)
+    ms_batch = timed(batch.render, steps, warmup)
     rays = sum(st.num_primary_rays + st.num_shadow_rays + st.num_path_rays
                for st in (batch.stats(i) for i in range(len(reqs))))
-    ms_solo = timed(solo_all, max(1, args.steps // 2), 1)
+    ms_solo = timed(solo_all, max(1, steps // 2), 1)
     out = {"metric": "Mrays/s, batched render requests (chosen form)", "value": round(rays / (ms_batch * 1e-3) / 1e6, 3),
-           "unit": "Mrays/s", "ms_per_step": round(ms_batch, 3), "steps": args.steps, "warmup": args.warmup,
+           "unit": "Mrays/s", "ms_per_step": round(ms_batch, 3), "steps": steps, "warmup": warmup,
            "requests": len(reqs), "rays_per_step": int(rays), "graph_kernels": batch.kernels(),
            "unbatched": {"value": round(rays / (ms_solo * 1e-3) / 1e6, 3), "ms_per_step": round(ms_solo, 3)},
            "batched_over_unbatched": round(ms_solo / ms_batch, 3),
            "scenes_triangles": [s[2] for s in scenes],
            "requests_by_resolution": {str(r): sum(1 for q in specs if q["width"] == r) for r in (128, 256, 512, 1024)}}
-    print(json.dumps(out))
+    batch.close()
+    for r, *_ in solos:
+        r.close()
+    return out
+
+
+def run_batched(args):
+    import torch
+
+    import vulkanwavefrontpathtracer_gb300 as wf
+    from vulkanwavefrontpathtracer_gb300 import build as wbuild
+    wbuild.build()
+    dev = torch.device("cuda", 0)
+    print(json.dumps(batched_serving(wf.api, dev, torch.cuda.current_stream(), args.batch_requests, args.steps,
+                                     args.warmup)))
+
+
+def sort_row(api, dev, stream, n=1 << 26, reps=5):
+    """Radix sorts of n uniform random pairs, u64 keys (63 bits, 8 passes)
+    and u32 keys (4 passes), u32 values: algorithmic GB/s (passes x 2 x
+    (key + value bytes) per pair) against the measured HBM peak."""
+    import torch
+    hbm, _ = peaks()
+    gen = torch.Generator(device=dev)
+    out = {"pairs": n}
+    for bits in (63, 32):
+        wide = bits > 32
+        gen.manual_seed(n + bits)
+        src = torch.randint(0, (1 << 62) if wide else (1 << 32), (n,), generator=gen, device=dev, dtype=torch.int64)
+        src = (src * 2 + (src & 1)) if wide else src.to(torch.int32)
+        keys = torch.empty_like(src)
+        vals = torch.arange(n, dtype=torch.int32, device=dev)
+        scratch = torch.empty(api.sort_scratch_bytes(n, 64 if wide else 32), dtype=torch.uint8, device=dev)
+
+        def timed(fn):
+            for _ in range(2):
+                fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        ms = timed(lambda: (keys.copy_(src), api.sort_pairs(keys, vals, bits, scratch=scratch)))
+        ms -= timed(lambda: keys.copy_(src))
+        passes = (bits + 7) // 8
+        gbs = passes * 2 * ((8 if wide else 4) + 4) * n / (ms * 1e-3) / 1e9
+        out["u64" if wide else "u32"] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 3),
+                                         "alg_bytes_per_pair": passes * 2 * ((8 if wide else 4) + 4)}
+        del src, keys, vals, scratch
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_sort_micro(args):
