@@ -150,6 +150,8 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          device allocation after n more successful ones
  *                          report WFPT_ERR_OUT_OF_MEMORY (nothing is
  *                          allocated); -1 (default) off
+ *   "debug.alloc_count"   read only (wfpt_tune_get): device and pinned host
+ *                          allocations the library has made in this process
  *   "trace.count"         1 = launch the counting traversal kernels, which
  *                          accumulate the counters read by wfpt_trace_counters
  *   "renderer.shadow_slots"  shadow batches a renderer runs at once in an

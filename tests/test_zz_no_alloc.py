@@ -73,8 +73,10 @@ def test_static_scratch_matches_caller_scratch_twice(wf, orc, dev, scene):
         inp = _inputs(orc, scene, n, seed)
         ref = _run(wf, dev, wf.api.raygen_path, geom, inp, n)
         l0 = wf._lib.load().wfpt_kernel_launch_count()
+        a0 = wf.api.tune_get("debug.alloc_count")
         got = _run(wf, dev, wf.api.raygen_path_static, geom, inp, n)
         assert wf._lib.load().wfpt_kernel_launch_count() - l0 == 1
+        assert wf.api.tune_get("debug.alloc_count") == a0  # the library allocated nothing
         assert 0 < ref[0] < n
         assert got[0] == ref[0]
         assert np.array_equal(bits(got[1]), bits(ref[1]))
@@ -142,7 +144,9 @@ def test_static_scratch_top_of_array_and_empty(wf, dev, scene):
     n = wf.api.RAYGEN_PATH_STATIC_MAX_RAYS
     inp = _synthetic_inputs(n, ntri, dev, 7)
     ref = _run_dev(wf.api.raygen_path, geom, inp, n)
+    a0 = wf.api.tune_get("debug.alloc_count")
     got = _run_dev(wf.api.raygen_path_static, geom, inp, n)
+    assert wf.api.tune_get("debug.alloc_count") == a0
     assert 0 < ref[0] < n
     assert got[0] == ref[0]
     for a, b in zip(got[1:], ref[1:]):
@@ -193,3 +197,22 @@ def test_static_scratch_first_call_under_capture_is_refused(wf):
                        timeout=300, env=dict(os.environ))
     assert r.returncode == 0, r.stdout + r.stderr
     assert "capture-check-ok" in r.stdout
+
+
+def test_allocation_counter_sees_library_allocations(wf, dev, scene):
+    """The counter the tests above rely on does count the library's own
+    device allocations: a renderer sizing its buffers for a first frame
+    raises it."""
+    import torch
+    pos, nrm, idx, nodes, tris = scene
+    sc = wf.api.Scene(pos, idx)
+    geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+    r = wf.api.Renderer(ray_type=wf.PATH_RAYS, recursion_depth=1, bvh_kind=wf.BVH8_Q8)
+    r.set_scene(sc, geom, (0.5, 1.6, 0.5), (0.5, 0.8, 0.9))
+    px = torch.zeros((32 * 32, 4), dtype=torch.float32, device=dev)
+    a0 = wf.api.tune_get("debug.alloc_count")
+    r.render(wf.api.make_camera(position=(0.5, 0.5, 2.2)), 32, 32, px, px.clone())
+    torch.cuda.synchronize()
+    assert wf.api.tune_get("debug.alloc_count") > a0
+    r.close()
+    sc.close()

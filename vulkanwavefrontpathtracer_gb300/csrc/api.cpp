@@ -125,6 +125,7 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_sort_digit_bits((int)value);
         return WFPT_OK;
     }
+    if (k == "debug.alloc_count") return invalid("debug.alloc_count is read-only");
     if (k == "debug.fail_alloc_after") {
         if (value < -1 || value > (1 << 20)) return invalid("debug.fail_alloc_after must be in [-1, 2^20]");
         wfpt::set_fail_alloc_after((int)value);
@@ -194,6 +195,10 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
     }
     if (k == "sort.digit_bits") {
         *value = wfpt::get_sort_digit_bits();
+        return WFPT_OK;
+    }
+    if (k == "debug.alloc_count") {
+        *value = (int64_t)wfpt::alloc_count();
         return WFPT_OK;
     }
     if (k == "debug.fail_alloc_after") {
@@ -474,7 +479,7 @@ wfpt_status wfpt_fill_u32(void* dst, uint32_t pattern, size_t count_u32, void* s
 
 // ------------------------------------------------------------- scene
 static cudaError_t upload(void** dst, const void* src, size_t bytes) {
-    cudaError_t e = cudaMalloc(dst, bytes);
+    cudaError_t e = wfpt::dev_malloc(dst, bytes);
     if (e != cudaSuccess) return e;
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
 }
@@ -534,7 +539,7 @@ static wfpt_status create_device_built(const float* positions_dev, uint32_t num_
     sc->bufs[2] = b.bvh8_nodes;
     sc->bufs[3] = b.bvh8_tris;
     sc->bufs[5] = b.rec_of_key;
-    e = cudaMalloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+    e = wfpt::dev_malloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(sc->bufs[4], 0, wfpt::kWorkSlots * 16 * sizeof(uint32_t));
     if (e != cudaSuccess) {
         wfpt_scene_destroy(sc);
@@ -663,7 +668,7 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
             sc->dev.bvh8_num_tris = (uint32_t)b8.tris.size();
         }
         if (e == cudaSuccess && !sc->host_only) {
-            e = cudaMalloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
+            e = wfpt::dev_malloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
             if (e == cudaSuccess) e = cudaMemset(sc->bufs[4], 0, wfpt::kWorkSlots * 16 * sizeof(uint32_t));
             sc->dev.work = reinterpret_cast<uint32_t*>(sc->bufs[4]);
         }

@@ -740,7 +740,7 @@ __global__ void __launch_bounds__(kBB) k_emit_write(const uint2* __restrict__ ta
 
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
-    return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(1, count) * sizeof(T));
+    return dev_malloc(reinterpret_cast<void**>(p), std::max<size_t>(1, count) * sizeof(T));
 }
 
 unsigned blocks(uint64_t n) { return (unsigned)((n + kBB - 1) / kBB); }

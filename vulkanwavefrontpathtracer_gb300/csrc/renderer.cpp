@@ -58,7 +58,7 @@ struct DevBuf {
         while (left >= 0 && !g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {
         }
         if (left == 0) return cudaErrorMemoryAllocation;
-        cudaError_t e = cudaMalloc(&p, b);
+        cudaError_t e = wfpt::dev_malloc(&p, b);
         if (e == cudaSuccess) bytes = b;
         return e;
     }
@@ -221,7 +221,9 @@ struct wfpt_renderer {
     cudaError_t render_graph(const float* s2w, const float* eye, float zfar, float* pixels, float* frame_pixels,
                              cudaStream_t s) {
         cudaError_t e;
-        if (!fp_dev && (e = cudaMalloc(&fp_dev, sizeof(wfpt::FrameParams))) != cudaSuccess) return e;
+        if (!fp_dev && (e = wfpt::dev_malloc(reinterpret_cast<void**>(&fp_dev), sizeof(wfpt::FrameParams))) !=
+                            cudaSuccess)
+            return e;
         if (!capture_stream && (e = cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
             return e;
         if ((e = wfpt::sort_prepare()) != cudaSuccess) return e;
@@ -435,7 +437,8 @@ struct wfpt_renderer {
             nslots = want;
         }
         if (!host_counters &&
-            (e = cudaMallocHost(&host_counters, (size_t)kMaxSamples * kCountersPerPass * 4)) != cudaSuccess)
+            (e = wfpt::host_malloc(reinterpret_cast<void**>(&host_counters), (size_t)kMaxSamples * kCountersPerPass * 4)) !=
+                cudaSuccess)
             return e;
         if (!ev0 && (e = cudaEventCreate(&ev0)) != cudaSuccess) return e;
         if (!ev1 && (e = cudaEventCreate(&ev1)) != cudaSuccess) return e;
@@ -1024,7 +1027,8 @@ wfpt_status wfpt_batch_create(const wfpt_request* requests, uint32_t count, int 
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
-    if (e == cudaSuccess) e = cudaMalloc(&b->fp_dev, (size_t)count * sizeof(wfpt::FrameParams));
+    if (e == cudaSuccess)
+        e = wfpt::dev_malloc(reinterpret_cast<void**>(&b->fp_dev), (size_t)count * sizeof(wfpt::FrameParams));
     if (e == cudaSuccess) e = wfpt::sort_prepare();
     if (e == cudaSuccess) e = wfpt::trace_prepare();
     if (e == cudaSuccess && !b->fill_params()) {

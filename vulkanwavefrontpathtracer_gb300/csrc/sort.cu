@@ -514,7 +514,7 @@ cudaError_t sort_selftest_timeout(cudaStream_t s) {
     if (e != cudaSuccess) return e;
     uint32_t* buf = nullptr;  // keys, values, keys out, values out, ticket, lookback
     const size_t words = 4 * (size_t)N + 1 + 2 * kRadix;
-    if ((e = cudaMalloc(&buf, words * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = dev_malloc(reinterpret_cast<void**>(&buf), words * sizeof(uint32_t))) != cudaSuccess) return e;
     uint32_t* keys = buf;
     uint32_t* vals = keys + N;
     uint32_t* keys_out = vals + N;

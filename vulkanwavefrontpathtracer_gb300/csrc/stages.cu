@@ -22,6 +22,17 @@ static std::atomic<uint64_t> g_launches{0};
 void count_launch(uint32_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+static std::atomic<uint64_t> g_allocs{0};
+cudaError_t dev_malloc(void** p, size_t bytes) {
+    g_allocs.fetch_add(1, std::memory_order_relaxed);
+    return cudaMalloc(p, bytes);
+}
+cudaError_t host_malloc(void** p, size_t bytes) {
+    g_allocs.fetch_add(1, std::memory_order_relaxed);
+    return cudaMallocHost(p, bytes);
+}
+uint64_t alloc_count() { return g_allocs.load(std::memory_order_relaxed); }
+
 // ---------------------------------------------------------------- seeds
 // initSeeds.comp:7-19 (TEA, 16 rounds) and :31-40.
 __device__ __forceinline__ uint32_t tea(uint32_t v0, uint32_t v1, uint32_t rounds) {
@@ -627,7 +638,7 @@ cudaError_t raygen_path_selftest_timeout(cudaStream_t s) {
     const size_t words = 3 * (size_t)N + 1 + 3;
     const size_t vec4s = 2 * (size_t)N * 2 + N + N;
     unsigned char* buf = nullptr;
-    cudaError_t e = cudaMalloc(&buf, vec4s * 16 + words * 4);
+    cudaError_t e = dev_malloc(reinterpret_cast<void**>(&buf), vec4s * 16 + words * 4);
     if (e != cudaSuccess) return e;
     float4* in_rays = reinterpret_cast<float4*>(buf);
     float4* out_rays = in_rays + 2 * N;

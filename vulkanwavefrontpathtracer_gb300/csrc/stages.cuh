@@ -69,6 +69,12 @@ cudaError_t launch_interpolate_colors_fp64(float* frame_pixels, float* pixels, d
                                            const FrameParams* fp = nullptr);
 // Host-side one-time set-up that must not happen inside a stream capture
 // (function attributes, occupancy queries).
+// Every device or pinned-host allocation the library makes goes through
+// these (cudaMalloc / cudaMallocHost); alloc_count() is the number made so
+// far in this process (tuning key "debug.alloc_count").
+cudaError_t dev_malloc(void** p, size_t bytes);
+cudaError_t host_malloc(void** p, size_t bytes);
+uint64_t alloc_count();
 cudaError_t sort_prepare();
 cudaError_t launch_fill_u32(void* dst, uint32_t v, size_t n, cudaStream_t s);
 cudaError_t launch_batch_count(const uint32_t* n_in_dev, uint32_t begin, uint32_t size, int S, uint32_t* out,
