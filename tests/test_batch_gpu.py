@@ -65,3 +65,55 @@ def test_batch_matches_standalone_renderers(wf, dev):
                    (b.num_primary_rays, b.num_shadow_rays, b.num_path_rays)
     assert wf.api.device_status() == 0
     batch.close()
+
+
+def test_batch_on_large_scenes_matches_oracle(wf, orc, dev):
+    """Batched requests on the batched workload's two city scenes (about 1M
+    and the 3,000,320-triangle block, their cameras and lights), chosen form,
+    small resolutions: every request's frame and ray counts equal the
+    oracle's CPU frame (FP32 BVH2 traversal of the same scene), bit for
+    bit."""
+    import sys
+    from pathlib import Path
+
+    import torch
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+    specs = [(2, 96, 64, 3, 1), (3, 64, 64, 2, 2)]  # (BATCH_SCENES index, w, h, depth, spp)
+    reqs, cases = [], []
+    for si, w, h, depth, spp in specs:
+        S = bench.BATCH_SCENES[si]
+        pos, nrm, idx = wf.api.generate_scene(S["kind"], S["seed"], S["ntris"])
+        sc = wf.api.Scene(pos, idx)
+        geom = wf.api.Geometry(pos, nrm, idx, device=dev)
+        over = dict(bench.COURTYARD["renderer"], recursion_depth=depth, num_primary_samples=spp)
+        cfg = wf.api.default_config(**over, **bench.CHOSEN)
+        px = torch.zeros((w * h, 4), dtype=torch.float32, device=dev)
+        fp = torch.zeros_like(px)
+        reqs.append(dict(scene=sc, geometry=geom, light=S["light"], background=S["background"],
+                         camera=wf.api.make_camera(**S["camera"]), width=w, height=h, config=cfg, pixels=px,
+                         frame_pixels=fp))
+        cases.append((S, pos, nrm, idx, sc, w, h, over))
+    batch = wf.api.Batch(reqs, streams=2)
+    batch.render()
+    torch.cuda.synchronize()
+    assert wf.api.device_status() == 0
+    for i, (S, pos, nrm, idx, sc, w, h, over) in enumerate(cases):
+        nodes, tris = sc.export_bvh2()
+        hg = orc.HostGeometry(wf.api.gltf_vertices(pos, nrm), idx)
+        c = S["camera"]
+        s2w = wf.api.camera_screen_to_world(c["position"], c["rotation_deg"], c["fov_deg"], w / h, c["znear"],
+                                            c["zfar"])
+        F = bench.CHOSEN
+        cfg = orc.FrameCfg(ray_type=2, spp=over["num_primary_samples"], S=over["num_shadow_samples"],
+                           depth=over["recursion_depth"], radius=over["shadow_radius"], key=over["key_value"],
+                           white=over["white_point"], albedo=over["albedo"], sort_shadow=F["sort_shadow_rays"],
+                           reorder_shadow=F["reorder_shadow_rays"], sort_path=F["sort_path_rays"],
+                           reorder_path=F["reorder_path_rays"], morton_kind=F["morton_kind"], frame_index=1)
+        o_px, o_fp, o_st = orc.render_frame(nodes, tris, hg, sc.bounds_min, sc.bounds_max, S["light"],
+                                            S["background"], s2w, c["position"], c["zfar"], w, h, cfg)
+        st = batch.stats(i)
+        assert (st.num_primary_rays, st.num_shadow_rays, st.num_path_rays) == (o_st.primary, o_st.shadow, o_st.path)
+        assert np.array_equal(_canon(reqs[i]["frame_pixels"].cpu().numpy()), _canon(o_fp)), i
+        assert np.array_equal(_canon(reqs[i]["pixels"].cpu().numpy()), _canon(o_px)), i
+    batch.close()
