@@ -438,6 +438,14 @@ def run_ours(args):
             "plain": {"value": round(plain_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_p / args.steps, 4),
                       "rays_per_frame": int(st_p.num_primary_rays + st_p.num_shadow_rays + st_p.num_path_rays)},
             "chosen_over_plain": round(value / plain_value, 3),
+            "chosen_over_plain_per_bounce": {
+                "courtyard_trace_only": micro["per_bounce"]["chosen_over_plain_trace_only"],
+                "courtyard_composite": micro["per_bounce"]["chosen_over_plain_composite"],
+                "city_trace_only": city_line["chosen_over_plain_trace_only"] if city_line else None,
+                "city_composite": city_line["chosen_over_plain_composite"] if city_line else None,
+                "note": "bounce-1 path rays (the incoherent bounce; city = the 3M-triangle block at 3840x2160): "
+                        "trace only = BVH8 on the sorted rays vs FP32 BVH2 on the unsorted rays; composite adds "
+                        "the Morton keys, sort and reorder to the chosen form"},
             "autotuned": {"value": round(tuned_value, 3), "unit": "Mrays/s", "ms_per_step": round(ms_t / args.steps, 4),
                           "over_plain": round(tuned_value / plain_value, 3), "path_sort_skip": mask,
                           "bvh_kind": bkind, "primary_bvh_kind": pkind,

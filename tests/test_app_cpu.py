@@ -45,6 +45,13 @@ def test_env_options_and_defaults(app):
     assert cfg.primary_bvh_kind == -1 and cfg.shadow_overlap == 1
     o2 = app.load_env(dict(ENV, Renderer=dict(ENV["Renderer"], primaryBvh="bvh2")))
     assert app.renderer_config(o2).primary_bvh_kind == 0
+    # Stage timing follows the benchmark mode (Benchmark.stageTimes, default on); FP64 accumulation
+    # is an option of its own.
+    assert cfg.timing == 1 and cfg.accumulate_fp64 == 0  # ENV is in benchmark mode
+    assert app.renderer_config(app.load_env(dict(ENV, Application={"mode": "interactive"}))).timing == 0
+    fp64_env = dict(ENV, Renderer=dict(ENV["Renderer"], accumulateFp64=True))
+    assert app.renderer_config(app.load_env(fp64_env)).accumulate_fp64 == 1
+    assert app.renderer_config(app.load_env(dict(ENV, Benchmark={"stageTimes": False}))).timing == 0
 
 
 @pytest.mark.parametrize("bad", [{"Renderer": {"rayType": "photon"}}, {"Renderer": {"numberOfBounces": 3}},
