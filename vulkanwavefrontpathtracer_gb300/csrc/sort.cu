@@ -6,7 +6,8 @@
 //   1. one histogram kernel reads the keys once and builds the 256-bin digit
 //      histogram of every pass (the global digit bases);
 //   2. per pass, one kernel of 512-thread CTAs, two resident per SM: each takes
-//      the next tile from a ticket counter, ranks its keys with warp ballots
+//      the next tile from a ticket counter, has L2 prefetch a tile half a wave
+//      ahead, ranks its keys with warp ballots
 //      (stable: keys are ranked in input order), publishes its per-digit
 //      counts, stages the tile in shared memory in digit order, resolves the
 //      global digit offsets with a bounded decoupled look-back over earlier
@@ -60,6 +61,22 @@ __host__ __device__ __forceinline__ uint32_t pass_mask(int key_bits, int p, int 
 }
 __device__ __forceinline__ uint32_t digit_of(uint32_t k, int shift, uint32_t dmask) { return (k >> shift) & dmask; }
 __device__ __forceinline__ uint32_t digit_of(uint64_t k, int shift, uint32_t dmask) { return (uint32_t)(k >> shift) & dmask; }
+
+// Lanes of the warp whose tested bit equals this lane's (`bit` is the
+// lane's key digit masked to one bit): the ballot of the bit, complemented
+// under the lane's own predicate when the bit is clear.  Written in PTX so
+// that the predicate of the vote also selects the complement (measured 4-8 %
+// faster per sort than a branch-free select in C++).
+__device__ __forceinline__ uint32_t same_bit_lanes(uint32_t bit) {
+    uint32_t m;
+    asm("{\n\t.reg .pred q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "vote.sync.ballot.b32 %0, q, 0xffffffff;\n\t"
+        "@!q not.b32 %0, %0;\n\t}"
+        : "=r"(m)
+        : "r"(bit));
+    return m;
+}
 
 // Exclusive scan of one value per thread over the whole block (blockDim.x =
 // 32 * W); *total receives the block sum.  Every thread must call it.
@@ -147,6 +164,17 @@ static void launch_hist(const K* keys, uint32_t n, const uint32_t* n_dev, int pa
     }
 }
 
+// Bulk prefetch into L2 of `count` keys and values (cp.async.bulk.prefetch:
+// one instruction per array, 16-byte aligned start and size).  Arrays that
+// are not 16-byte aligned are skipped; the loads then go to DRAM as usual.
+template <typename K>
+__device__ __forceinline__ void prefetch_l2(const K* keys, const uint32_t* vals, uint32_t count) {
+    const uint32_t kb = count * (uint32_t)sizeof(K), vb = count * 4u;
+    if (((reinterpret_cast<uintptr_t>(keys) | reinterpret_cast<uintptr_t>(vals) | kb | vb) & 15u) != 0) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(keys), "r"(kb) : "memory");
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(vals), "r"(vb) : "memory");
+}
+
 // One tile of a digit pass (below).  FULL: the tile holds TILE keys, so
 // the per-key bounds checks of the last, partial tile drop out.
 template <typename K, int KPT, int DB, bool FULL>
@@ -182,11 +210,7 @@ __device__ __forceinline__ void onesweep_tile(const K* __restrict__ keys_in, con
         uint32_t d = digit_of(key[k], shift, dmask);
         uint32_t peers = FULL ? 0xffffffffu : __ballot_sync(0xffffffffu, ok);
 #pragma unroll
-        for (int b = 0; b < DB; ++b) {
-            uint32_t bit = (d >> b) & 1u;
-            uint32_t m = __ballot_sync(0xffffffffu, bit);
-            peers &= m ^ (bit - 1u);  // m where the bit is set, ~m where clear
-        }
+        for (int b = 0; b < DB; ++b) peers &= same_bit_lanes(d & (1u << b));
         uint32_t before = peers & lt_mask;
         uint32_t pre = ok ? my_hist[d] : 0u;
         __syncwarp();
@@ -289,8 +313,10 @@ __device__ __forceinline__ void onesweep_tile(const K* __restrict__ keys_in, con
         K kk = s_keys[j];
         uint32_t g = s_base[digit_of(kk, shift, dmask)] + j;
         if (g < count) {  // only fails after a look-back timeout
-            keys_out[g] = kk;
-            vals_out[g] = s_vals[j];
+            // Streaming stores: the output is next read by the following
+            // pass, after far more than L2 holds has gone through it.
+            __stcs(keys_out + g, kk);
+            __stcs(vals_out + g, s_vals[j]);
         } else {
             raise_status(kErrBounds);
         }
@@ -302,7 +328,10 @@ __device__ __forceinline__ void onesweep_tile(const K* __restrict__ keys_in, con
 // counters, RADIX global bases, RADIX local offsets.  hist is the byte
 // histogram (k_sort_hist) of this pass's byte; with 4-bit digits a digit's
 // count is the sum of the 16 byte bins sharing that nibble (nibble 0: low
-// nibble of the byte, 1: high nibble).
+// nibble of the byte, 1: high nibble).  The CTA that draws tile t asks L2
+// for the keys and values of tile t + lead (half the resident CTAs ahead:
+// the tile that starts about half a tile's lifetime later), so that a
+// tile's loads find their data in L2 instead of waiting on DRAM.
 template <typename K, int KPT, int DB>
 __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const K* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
@@ -311,7 +340,8 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
                                                               const uint32_t* __restrict__ n_dev, int shift,
                                                               uint32_t dmask, const uint32_t* __restrict__ hist,
                                                               uint32_t* __restrict__ lookback,
-                                                              uint32_t* __restrict__ ticket, int nibble) {
+                                                              uint32_t* __restrict__ ticket, int nibble,
+                                                              uint32_t lead) {
     constexpr uint32_t TILE = kSortThreads * KPT;
     constexpr int kRadix = 1 << DB;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -321,7 +351,13 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
 
     const uint32_t count = load_count(n, n_dev);
     const uint32_t ntiles = (count + TILE - 1) / TILE;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    if (threadIdx.x == 0) {
+        const uint32_t t = atomicAdd(ticket, 1u);
+        s_tile = t;
+        const uint32_t ahead = t + lead;
+        if (lead != 0 && ahead > t && (size_t)(ahead + 1) * TILE <= count)
+            prefetch_l2(keys_in + (size_t)ahead * TILE, vals_in + (size_t)ahead * TILE, TILE);
+    }
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -449,6 +485,10 @@ static cudaError_t sort_passes(K* keys, uint32_t* values, uint32_t n, const uint
     uint32_t* alt_vals = reinterpret_cast<uint32_t*>(scratch + L.off_vals);
     const uint32_t tiles = (n + TILE - 1) / TILE;
     const size_t smem = onesweep_smem<K, KPT, DB>();
+    // Prefetch distance in tiles: half the CTAs resident at once (measured
+    // 3/8 to 5/8 of them equally good at 2^24-2^26 pairs; a whole wave
+    // ahead was 6 % slower, two waves slower than no prefetch).
+    const uint32_t lead = (uint32_t)(g_num_sms * kSortCtasPerSm / 2);
     cudaError_t e;
     K* src_k = keys;
     uint32_t* src_v = values;
@@ -458,7 +498,7 @@ static cudaError_t sort_passes(K* keys, uint32_t* values, uint32_t n, const uint
         const int byte = DB == 8 ? p : p / 2;
         k_onesweep<K, KPT, DB><<<tiles, kSortThreads, smem, s>>>(
             src_k, src_v, dst_k, dst_v, n, n_dev, DB * p, pass_mask(key_bits, p, DB), hist + byte * kRadix,
-            lookback + (size_t)p * L.tiles * RADIX, tickets + p, DB == 8 ? 0 : (p & 1));
+            lookback + (size_t)p * L.tiles * RADIX, tickets + p, DB == 8 ? 0 : (p & 1), lead);
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(src_k, dst_k);
@@ -527,7 +567,7 @@ cudaError_t sort_selftest_timeout(cudaStream_t s) {
     if (e == cudaSuccess) {
         k_onesweep<uint32_t, KPT, 8><<<1, kSortThreads, onesweep_smem<uint32_t, KPT, 8>(), s>>>(
             keys, vals, keys_out, vals_out, N, nullptr, 0, 0xFFu, lookback /* unused for tile 1 */, lookback,
-            ticket, 0);
+            ticket, 0, 0u);
         count_launch();
         e = cudaGetLastError();
     }
