@@ -14,8 +14,8 @@
 //      tiles and writes keys and values out in coalesced runs.
 // Sized for a frame's wavefronts (a few million keys, all of it resident in
 // L2): tiles of 8 or 14-16 keys per thread make such a pass one wave of
-// about two tiles per SM, and the look-back reads 16 predecessors per L2
-// round trip, so the prefix crosses a wave in a handful of round trips;
+// about two tiles per SM, and the look-back reads 8 predecessors per L2
+// round trip with a cheap test for the common round of published aggregates;
 // staging the tile before the look-back overlaps that wait with useful work.
 // Ping-pong between the caller's buffers and scratch; after an even number
 // of passes the result is back in the caller's buffers (as in the reference),
@@ -42,7 +42,11 @@ constexpr int kHistBlock = 256;
 constexpr uint32_t kLbAggregate = 1u << 30;
 constexpr uint32_t kLbPrefix = 2u << 30;
 constexpr uint32_t kLbValue = (1u << 30) - 1u;
-constexpr int kLbChunk = 16;  // predecessors read per look-back round trip
+// Predecessors read per look-back round trip.  With the all-aggregates fast
+// path below, 8 measured 1-4 % faster per sort than 16 at 16.8M-67M pairs
+// and equal at 2.07M (24 and 32 slower): a round is bound by the owner
+// warps' instructions as much as by the L2 round trip.
+constexpr int kLbChunk = 8;
 
 // Keys per thread of the tile variants (tile = 512 * KPT keys).  The
 // extra-large variant serves sorts of more than two waves of large tiles:
@@ -109,6 +113,34 @@ __device__ __forceinline__ uint32_t key_byte(uint64_t k, int p) {
     return p < 4 ? ((uint32_t)k >> (8 * p)) & 0xFFu : ((uint32_t)(k >> 32) >> (8 * (p - 4))) & 0xFFu;
 }
 
+// Programmatic dependent launch between the sort's kernels.  A pass kernel
+// is launched with programmatic stream serialisation: its CTAs may start
+// once every CTA of the previous kernel has started (or exited) and run
+// their prologue (ticket, clearing the counters) while the previous kernel
+// finishes; wait_for_previous_grid() then blocks until that kernel has
+// completed and its writes are visible.  Nothing the previous kernel writes
+// is read before the wait.  At a frame's sort size (one wave of tiles per
+// pass) this hides the launch gap and the ticket round trip of every pass:
+// 10 % faster sorts of 2.07M u64 pairs, 7 % at 16.8M, 2.5 % at 67M.
+__device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void wait_for_previous_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename Kernel, typename... Args>
+static cudaError_t launch_dependent(Kernel kernel, unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Histogram of every pass's digit over the first `count` keys: PASSES is a
 // template parameter so that the digit extraction unrolls into constant
 // byte selects; each thread issues the loads of 8 keys before their
@@ -119,6 +151,9 @@ __global__ void __launch_bounds__(kHistBlock) k_sort_hist(const K* __restrict__ 
                                                            uint32_t* __restrict__ hist) {
     constexpr int U = 8;
     __shared__ uint32_t s_h[PASSES * kRadix];
+    // Every CTA of this grid has started: the first pass may launch its
+    // CTAs into the slots this grid frees (they wait for its completion).
+    allow_dependent_launch();
     for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistBlock) s_h[i] = 0;
     __syncthreads();
     const uint32_t count = load_count(n, n_dev);
@@ -283,6 +318,25 @@ __device__ __forceinline__ void onesweep_tile(const K* __restrict__ keys_in, con
             for (int q = 0; q < kLbChunk; ++q)
                 st[q] = (j - q >= 0) ? *((volatile uint32_t*)(lookback + (size_t)(j - q) * kRadix + d))
                                      : uint32_t(kLbPrefix);
+            // Fast path: every entry a published aggregate (flag bit 30 set
+            // in all of them; a prefix has bit 31 alone, an unpublished entry
+            // neither).  Their raw sum minus the flags is the sum of the
+            // counts, so the round costs an AND and an add per entry instead
+            // of the sequential scan (5-9 % faster sorts at the frame's 2.07M
+            // pairs, where most rounds are of this kind).
+            {
+                uint32_t all = 0xFFFFFFFFu, raw = 0u;
+#pragma unroll
+                for (int q = 0; q < kLbChunk; ++q) {
+                    all &= st[q];
+                    raw += st[q];
+                }
+                if (all & kLbAggregate) {
+                    excl += raw - (uint32_t)kLbChunk * kLbAggregate;
+                    j -= kLbChunk;
+                    continue;
+                }
+            }
             int used = 0;
 #pragma unroll
             for (int q = 0; q < kLbChunk; ++q) {
@@ -349,16 +403,21 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) k_onesweep(const
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_scan[kSortWarps];
 
+    // Prologue that reads nothing the previous kernel writes (the tickets
+    // and look-back states of this pass were cleared before the sort began).
+    uint32_t t = 0;
+    if (threadIdx.x == 0) t = atomicAdd(ticket, 1u);
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
+    allow_dependent_launch();
+    wait_for_previous_grid();
     const uint32_t count = load_count(n, n_dev);
     const uint32_t ntiles = (count + TILE - 1) / TILE;
     if (threadIdx.x == 0) {
-        const uint32_t t = atomicAdd(ticket, 1u);
         s_tile = t;
         const uint32_t ahead = t + lead;
         if (lead != 0 && ahead > t && (size_t)(ahead + 1) * TILE <= count)
             prefetch_l2(keys_in + (size_t)ahead * TILE, vals_in + (size_t)ahead * TILE, TILE);
     }
-    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) s_hist[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
     if (tile >= ntiles) return;
@@ -496,11 +555,12 @@ static cudaError_t sort_passes(K* keys, uint32_t* values, uint32_t n, const uint
     uint32_t* dst_v = alt_vals;
     for (int p = 0; p < passes; ++p) {
         const int byte = DB == 8 ? p : p / 2;
-        k_onesweep<K, KPT, DB><<<tiles, kSortThreads, smem, s>>>(
-            src_k, src_v, dst_k, dst_v, n, n_dev, DB * p, pass_mask(key_bits, p, DB), hist + byte * kRadix,
-            lookback + (size_t)p * L.tiles * RADIX, tickets + p, DB == 8 ? 0 : (p & 1), lead);
+        e = launch_dependent(k_onesweep<K, KPT, DB>, tiles, kSortThreads, smem, s, (const K*)src_k,
+                             (const uint32_t*)src_v, dst_k, dst_v, n, n_dev, (int)(DB * p), pass_mask(key_bits, p, DB),
+                             (const uint32_t*)(hist + byte * kRadix), lookback + (size_t)p * L.tiles * RADIX,
+                             tickets + p, (int)(DB == 8 ? 0 : (p & 1)), lead);
         count_launch();
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(src_k, dst_k);
         std::swap(src_v, dst_v);
     }
