@@ -44,7 +44,7 @@ struct wfpt_scene {
     wfpt::HostBvh2 bvh2;  // plain-form BVH kept on the host for export
     wfpt::HostBvh8 bvh8;
     wfpt::SceneDevice dev;
-    void* bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void* bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     wfpt_scene_info info{};
     bool has2 = false, has8 = false, host_only = false;
     bool device_built = false;  // BVHs built on the GPU: no host copies
@@ -522,7 +522,7 @@ static wfpt_status create_device_built(const float* positions_dev, uint32_t num_
     }
     wfpt_scene* sc = new (std::nothrow) wfpt_scene();
     if (!sc) {
-        for (void* p : {b.bvh2_nodes, b.bvh2_tris, b.bvh8_nodes, b.bvh8_tris, b.rec_of_key})
+        for (void* p : {b.bvh2_nodes, b.bvh2_tris, b.bvh8_nodes, b.bvh8_tris})
             if (p) cudaFree(p);
         return WFPT_ERR_OUT_OF_MEMORY;
     }
@@ -538,7 +538,6 @@ static wfpt_status create_device_built(const float* positions_dev, uint32_t num_
     }
     sc->bufs[2] = b.bvh8_nodes;
     sc->bufs[3] = b.bvh8_tris;
-    sc->bufs[5] = b.rec_of_key;
     e = wfpt::dev_malloc(&sc->bufs[4], wfpt::kWorkSlots * 16 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(sc->bufs[4], 0, wfpt::kWorkSlots * 16 * sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -550,7 +549,6 @@ static wfpt_status create_device_built(const float* positions_dev, uint32_t num_
     sc->dev.bvh2_tris = reinterpret_cast<const float4*>(sc->bufs[1]);
     sc->dev.bvh8_nodes = reinterpret_cast<const float4*>(sc->bufs[2]);
     sc->dev.bvh8_tris = reinterpret_cast<const float4*>(sc->bufs[3]);
-    sc->dev.bvh8_rec_of_key = reinterpret_cast<const uint32_t*>(sc->bufs[5]);
     sc->dev.bvh8_num_tris = sc->has8 ? num_triangles : 0u;
     sc->dev_bvh2_count = sc->has2 ? b.bvh2_count : 0u;
     sc->dev_bvh8_count = sc->has8 ? b.bvh8_count : 0u;
@@ -633,7 +631,6 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
                         num_geometries == 0 ? 1u : num_geometries};
     try {
         wfpt::HostBvh2 for8;
-        std::vector<uint32_t> rec_of_key;
         if (bvh_kinds_mask & (1 << WFPT_BVH2_FP32)) {
             wfpt::build_bvh2(in, 4, sc->bvh2);
             sc->has2 = true;
@@ -644,12 +641,6 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
             wfpt::build_bvh8(for8, b8);
             sc->has8 = true;
             if (!sc->has2) sc->bvh2 = for8;
-            // rec_of_key[global triangle index] = BVH8 record.  An empty
-            // scene holds one zeroed placeholder record that no ray can hit;
-            // the table keeps at least one entry.
-            rec_of_key.assign(num_triangles ? num_triangles : 1u, 0u);
-            for (size_t i = 0; i < b8.tris.size(); ++i)
-                if (b8.tris[i].global < num_triangles) rec_of_key[b8.tris[i].global] = (uint32_t)i;
         }
         sc->host_only = (bvh_kinds_mask & WFPT_SCENE_HOST_ONLY) != 0;
         cudaError_t e = cudaSuccess;
@@ -663,8 +654,6 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
         if (e == cudaSuccess && sc->has8 && !sc->host_only) {
             e = upload(&sc->bufs[2], b8.nodes.data(), b8.nodes.size() * sizeof(wfpt::Bvh8Node));
             if (e == cudaSuccess) e = upload(&sc->bufs[3], b8.tris.data(), b8.tris.size() * sizeof(wfpt::TriRec));
-            if (e == cudaSuccess)
-                e = upload(&sc->bufs[5], rec_of_key.data(), rec_of_key.size() * sizeof(uint32_t));
             sc->dev.bvh8_num_tris = (uint32_t)b8.tris.size();
         }
         if (e == cudaSuccess && !sc->host_only) {
@@ -680,7 +669,6 @@ wfpt_status wfpt_scene_create(const float* positions, uint32_t num_vertices, con
         sc->dev.bvh2_tris = reinterpret_cast<const float4*>(sc->bufs[1]);
         sc->dev.bvh8_nodes = reinterpret_cast<const float4*>(sc->bufs[2]);
         sc->dev.bvh8_tris = reinterpret_cast<const float4*>(sc->bufs[3]);
-        sc->dev.bvh8_rec_of_key = reinterpret_cast<const uint32_t*>(sc->bufs[5]);
         sc->info.num_triangles = num_triangles;
         sc->info.num_geometries = num_geometries == 0 ? 1 : num_geometries;
         sc->info.bvh2_nodes = sc->has2 ? (uint32_t)sc->bvh2.nodes.size() : 0;

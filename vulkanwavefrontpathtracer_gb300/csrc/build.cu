@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(kBB) k_emit_write(const uint2* __restrict__ ta
                                                     const int8_t* __restrict__ how, const int8_t* __restrict__ split8,
                                                     const uint32_t* __restrict__ ntris,
                                                     const float4* __restrict__ recs2, Bvh8Node* __restrict__ out,
-                                                    float4* __restrict__ recs8, uint32_t* __restrict__ rec_of_key,
+                                                    float4* __restrict__ recs8,
                                                     uint2* __restrict__ next_tasks) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
@@ -722,8 +722,6 @@ __global__ void __launch_bounds__(kBB) k_emit_write(const uint2* __restrict__ ta
                 recs8[3 * (size_t)dst] = a;
                 recs8[3 * (size_t)dst + 1] = b;
                 recs8[3 * (size_t)dst + 2] = cc;
-                const uint32_t key = __float_as_uint(cc.w);
-                if (key < tri_cap) rec_of_key[key] = dst;
             }
             tri_off += (uint32_t)cnt;
         } else {
@@ -769,7 +767,6 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
     Bvh2Node* nodes2 = nullptr;
     float4* recs2 = nullptr;
     float4* recs8 = nullptr;
-    uint32_t* rok = nullptr;
     Bvh8Node* nodes8 = nullptr;
     const size_t ninner = (size_t)n - 1, nall = 2 * (size_t)n - 1;
     const size_t sort_bytes = sort_scratch_bytes(n, 63);
@@ -889,7 +886,6 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
         WFPT_TRY(dalloc(&tasks2, ninner));
         WFPT_TRY(dalloc(&nodes8_tmp, ninner));
         WFPT_TRY(dalloc(&recs8, 3 * (size_t)n));
-        WFPT_TRY(dalloc(&rok, n));
         WFPT_TRY(cudaMemsetAsync(visits, 0, ninner * sizeof(uint32_t), s));
         k_collapse_dp<<<blocks(n), kBB, 0, s>>>(n, nodes2, parent, visits, cost, how, split8, ntris,
                                                 (float)get_bvh8_tri_cost_pct() * 0.01f);
@@ -909,7 +905,7 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
             WFPT_TRY(exclusive_scan(flags, excl, ntasks, scan, s));
             k_emit_write<<<blocks(ntasks), kBB, 0, s>>>(tasks, ntasks, excl, node_count, tri_count,
                                                         (uint32_t)ninner, n, nodes2, how, split8, ntris, recs2,
-                                                        nodes8_tmp, recs8, rok, tasks2);
+                                                        nodes8_tmp, recs8, tasks2);
             count_launch();
             WFPT_TRY(cudaGetLastError());
             WFPT_TRY(cudaMemcpyAsync(&host_total, total, sizeof(host_total), cudaMemcpyDeviceToHost, s));
@@ -946,19 +942,17 @@ cudaError_t build_scene_device(const float* positions_dev, uint32_t num_vertices
     out->bvh2_count = (uint32_t)ninner;
     out->bvh8_nodes = nodes8;
     out->bvh8_tris = recs8;
-    out->rec_of_key = rok;
     nodes2 = nullptr;
     recs2 = nullptr;
     nodes8 = nullptr;
     recs8 = nullptr;
-    rok = nullptr;
 #undef WFPT_TRY
 done:
     for (void* p : {(void*)tlo, (void*)thi, (void*)nlo, (void*)nhi, (void*)keys, (void*)flags, (void*)excl,
                     (void*)bsums, (void*)total, (void*)vals, (void*)cl, (void*)cl2, (void*)nn, (void*)parent,
                     (void*)kids, (void*)st, (void*)sort_scratch, (void*)cost, (void*)how, (void*)split8,
                     (void*)ntris, (void*)visits, (void*)tasks, (void*)tasks2, (void*)nodes8_tmp, (void*)nodes2,
-                    (void*)recs2, (void*)recs8, (void*)rok, (void*)nodes8})
+                    (void*)recs2, (void*)recs8, (void*)nodes8})
         if (p) cudaFree(p);
     return e;
 }

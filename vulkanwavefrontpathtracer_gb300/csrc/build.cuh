@@ -13,7 +13,6 @@ struct DeviceBuild {
     void* bvh2_tris = nullptr;   // TriRec[num_triangles]
     void* bvh8_nodes = nullptr;  // Bvh8Node[bvh8_count]
     void* bvh8_tris = nullptr;   // TriRec[num_triangles]
-    void* rec_of_key = nullptr;  // uint32[num_triangles]
     uint32_t bvh2_count = 0, bvh8_count = 0;
     float bounds_min[3] = {0, 0, 0}, bounds_max[3] = {0, 0, 0};
     uint32_t ploc_iterations = 0;

@@ -92,9 +92,6 @@ struct SceneDevice {
     const float4* bvh2_tris = nullptr;
     const float4* bvh8_nodes = nullptr;
     const float4* bvh8_tris = nullptr;
-    // rec_of_key[global triangle index] = BVH8 triangle record (each
-    // triangle has exactly one record).
-    const uint32_t* bvh8_rec_of_key = nullptr;
     uint32_t bvh8_num_tris = 0;
     uint32_t* work = nullptr;
 };

