@@ -77,11 +77,11 @@ METRIC = "Mrays/s per bounce, chosen vs plain form; radix sort+reorder HBM GB/s 
 TRACE_DRAM_BYTES_PER_RAY = {"any": 46.64, "closest": 47.20}
 # Warp instructions per ray of the courtyard's bounce-1 BVH8 traversal
 # (sm__inst_executed.sum / rays of one launch each, `bench.py --trace-profile`
-# under ncu at 960x540: 284,186,300 for 518,400 sorted closest-hit path rays,
-# 338,336,587 for 1,036,800 any-hit shadow rays).  With the live launch time
+# under ncu at 960x540: 288,619,160 for 518,400 sorted closest-hit path rays,
+# 337,241,928 for 1,036,800 any-hit shadow rays).  With the live launch time
 # they give the issue rate; the issue peak is 152 SMs x 4 schedulers x one
 # warp instruction per clock at the sampled SM clock.
-TRACE_WARP_INST_PER_RAY = {"any": 326.33, "closest": 548.20}
+TRACE_WARP_INST_PER_RAY = {"any": 325.27, "closest": 556.75}
 NUM_SMS = 152
 
 
