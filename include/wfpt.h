@@ -227,7 +227,13 @@ size_t wfpt_sort_scratch_bytes(uint32_t max_n, int key_bits);
  * vk_radix_sort.h:2579-2585).  Keys are uint32_t when key_bits <= 32, else
  * uint64_t; only the low key_bits bits are sorted on (ceil(key_bits/8)
  * passes).  The result is left in keys/values, like the reference.  Values
- * are uint32.  Ordering equals a stable sort by key. */
+ * are uint32.  Ordering equals a stable sort by key.  The call enqueues a
+ * memset of the scratch, a histogram kernel and one kernel per pass; the
+ * pass kernels are launched with programmatic stream serialisation after
+ * the library's own previous kernel (they start as it drains and wait for
+ * it before reading), so a stream capture records programmatic edges
+ * between them.  Work the caller enqueues after the sort starts only when
+ * the sort has completed, as with any stream-ordered call. */
 wfpt_status wfpt_sort_pairs(void* keys, uint32_t* values, uint32_t n,
                             const uint32_t* n_dev, int key_bits, void* scratch,
                             size_t scratch_bytes, void* stream);

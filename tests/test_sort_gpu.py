@@ -152,6 +152,43 @@ def test_sort_tile_variants(wf, dev, tiles, n, key_bits, digit_bits):
     assert wf.api.device_status() == 0
 
 
+@pytest.mark.parametrize("key_bits,n", [(63, 2073600), (63, 5000000), (32, 3000001)])
+def test_sort_captured_graph_replays(wf, dev, key_bits, n):
+    """The sort captured into a CUDA graph (its passes are launched as
+    programmatic dependents of the kernel before them, which capture turns
+    into programmatic edges) and replayed on new keys copied into the
+    captured buffers: every replay gives the stable order.  Sizes of one
+    wave of tiles and of several."""
+    import torch
+    is64 = key_bits > 32
+    kt = torch.int64 if is64 else torch.int32
+    keys = torch.zeros(n, dtype=kt, device=dev)
+    vals = torch.zeros(n, dtype=torch.int32, device=dev)
+    scratch = torch.empty(wf.api.sort_scratch_bytes(n, key_bits), dtype=torch.uint8, device=dev)
+    iota = torch.arange(n, dtype=torch.int32, device=dev)
+    wf.api.sort_pairs(keys, vals, key_bits, scratch=scratch)  # prepares the kernels outside the capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        wf.api.sort_pairs(keys, vals, key_bits, scratch=scratch, stream=s)
+    rng = np.random.default_rng(key_bits + n)
+    for rep in range(3):
+        if is64:
+            src = rng.integers(0, 2**63, n, dtype=np.uint64)
+        else:
+            src = rng.integers(0, 2**32, n, dtype=np.uint32)
+        src[:: 4 + rep] = src[7]  # duplicates: stability matters
+        keys.copy_(T(src.view(np.int64 if is64 else np.int32), dev))
+        vals.copy_(iota)
+        g.replay()
+        torch.cuda.synchronize()
+        rk, rv = stable_ref(src, key_bits)
+        assert np.array_equal(N(vals).view(np.uint32), rv), rep
+        assert np.array_equal(N(keys).view(np.uint64 if is64 else np.uint32), rk), rep
+    assert wf.api.device_status() == 0
+
+
 @pytest.mark.parametrize("key_bits", [63, 32])
 def test_sort_unaligned_buffers(wf, dev, key_bits):
     """Caller buffers one element past a 16-byte boundary: the passes that
