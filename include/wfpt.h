@@ -369,7 +369,7 @@ wfpt_status wfpt_interpolate_colors(float* frame_pixels, float* pixels,
                                     void* stream);
 
 /* interpolateColors.comp:71-98 with the running mean kept in double
- * (the benchmark spec's FP64 per-pixel accumulation): accum holds one double4
+ * (FP64 per-pixel accumulation over frames): accum holds one double4
  * per pixel (xyz the mean, w unused; 32-byte aligned), written on every
  * frame (frame 1: the frame's colour), blended on later frames with
  * a = 1/frame, b = a * (frame - 1) in double; pixels receives the mean

@@ -661,8 +661,8 @@ extern "C" void orc_interpolate_colors(float* frame_pixels, float* pixels, uint3
     }
 }
 
-// The same running mean kept in double (the benchmark spec's FP64 per-pixel
-// accumulation): accum holds 4 doubles per pixel; a = 1/frame and
+// The same running mean kept in double (FP64 per-pixel accumulation over
+// frames): accum holds 4 doubles per pixel; a = 1/frame and
 // b = a * (frame - 1) in double; pixels gets the mean rounded to float (w
 // as the shader writes it) and the tone map (float) reads that rounding.
 extern "C" void orc_interpolate_colors_fp64(float* frame_pixels, float* pixels, double* accum, uint32_t n,
