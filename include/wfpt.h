@@ -129,12 +129,15 @@ uint64_t wfpt_kernel_launch_count(void);
  *                          0 = each lane tests its own.  Closest hits are
  *                          identical; an any-hit ray may report a different
  *                          (equally valid) occluder
- *   "trace.bvh8.batch"     cooperative tests: run them once this many are
- *                          pending across the warp's node steps (1..32,
- *                          default 16; 1 = after every node step)
- *   "trace.bvh8.steps"     cooperative tests: node steps a lane takes per
- *                          loop iteration while its steps hand it no
- *                          triangles (1..8, default 2)
+ *   "trace.bvh8.batch"     cooperative tests of closest-hit rays: run them
+ *                          once this many are pending across the warp's
+ *                          node steps (1..32, default 24; 1 = after every
+ *                          loop iteration)
+ *   "trace.bvh8.steps"     cooperative tests of closest-hit rays: node steps
+ *                          a lane takes per loop iteration while its steps
+ *                          hand it no triangles (1..8, default 2)
+ *   "trace.bvh8.any_batch" the same for any-hit rays (default 1)
+ *   "trace.bvh8.any_steps" the same for any-hit rays (default 3)
  *   "sort.tiles"           radix sort tile size: 0 = by problem size
  *                          (default), 1 = small tiles, 2 = large tiles,
  *                          3 = extra-large tiles (32-bit keys; 64-bit keys

@@ -297,20 +297,28 @@ def test_cpu_frame_runs(wf, orc):
 def test_tuning_knobs(wf):
     api = wf.api
     old = (api.tune_get("trace.bvh8.refill"), api.tune_get("trace.bvh8.postpone"), api.tune_get("trace.bvh8.coop"),
-           api.tune_get("trace.bvh8.batch"), api.tune_get("trace.bvh8.steps"))
-    assert old[2] == 1 and old[3] == 16 and old[4] == 2  # cooperative, batched triangle tests by default
+           api.tune_get("trace.bvh8.batch"), api.tune_get("trace.bvh8.steps"), api.tune_get("trace.bvh8.any_batch"),
+           api.tune_get("trace.bvh8.any_steps"))
+    # cooperative tests by default: batched over two node steps for closest-hit rays, after every
+    # iteration of three node steps for any-hit rays
+    assert old[2] == 1 and old[3] == 24 and old[4] == 2 and old[5] == 1 and old[6] == 3
     try:
         api.tune_set("trace.bvh8.refill", 4)
         api.tune_set("trace.bvh8.postpone", 6)
         api.tune_set("trace.bvh8.coop", 0)
         api.tune_set("trace.bvh8.batch", 9)
         api.tune_set("trace.bvh8.steps", 3)
+        api.tune_set("trace.bvh8.any_batch", 7)
+        api.tune_set("trace.bvh8.any_steps", 5)
+        assert api.tune_get("trace.bvh8.any_batch") == 7 and api.tune_get("trace.bvh8.any_steps") == 5
+        assert api.tune_get("trace.bvh8.batch") == 9  # the kinds are independent
         assert api.tune_get("trace.bvh8.refill") == 4 and api.tune_get("trace.bvh8.postpone") == 6
         assert api.tune_get("trace.bvh8.coop") == 0 and api.tune_get("trace.bvh8.batch") == 9
         assert api.tune_get("trace.bvh8.steps") == 3
         for key, bad in (("trace.bvh8.refill", 0), ("trace.bvh8.refill", 33), ("trace.bvh8.postpone", -1),
                          ("trace.bvh8.batch", 0), ("trace.bvh8.batch", 33), ("trace.bvh8.steps", 0),
-                         ("trace.bvh8.steps", 9),
+                         ("trace.bvh8.steps", 9), ("trace.bvh8.any_batch", 0), ("trace.bvh8.any_batch", 33),
+                         ("trace.bvh8.any_steps", 0), ("trace.bvh8.any_steps", 9),
                          ("trace.bvh8.coop", 2), ("sort.tiles", 4), ("sort.tiles", -1), ("sort.digit_bits", 5), ("sort.digit_bits", 16), ("build.bvh8.collapse", 2),
                          ("build.bvh8.tri_cost", 0), ("build.bvh8.tri_cost", 10001), ("build.ploc.radius", 0),
                          ("build.ploc.radius", 65), ("debug.fail_alloc_after", -2), ("no.such.knob", 1)):
@@ -322,6 +330,8 @@ def test_tuning_knobs(wf):
         api.tune_set("trace.bvh8.coop", old[2])
         api.tune_set("trace.bvh8.batch", old[3])
         api.tune_set("trace.bvh8.steps", old[4])
+        api.tune_set("trace.bvh8.any_batch", old[5])
+        api.tune_set("trace.bvh8.any_steps", old[6])
 
 
 def test_batch_arguments_rejected_on_host(wf):

@@ -200,10 +200,10 @@ def test_bvh8_batched_tests_indirect_device_count(wf, dev, soup, batch, steps, c
     rays[::7, 7] = -1.0  # tmax < tmin: miss
     perm = rng.permutation(n).astype(np.uint32)
     ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=closest)
-    keys = ("trace.bvh8.batch", "trace.bvh8.steps")
+    keys = ("trace.bvh8.batch", "trace.bvh8.steps", "trace.bvh8.any_batch", "trace.bvh8.any_steps")
     old = [wf.api.tune_get(k) for k in keys]
     try:
-        for k, v in zip(keys, (batch, steps)):
+        for k, v in zip(keys, (batch, steps, batch, steps)):
             wf.api.tune_set(k, v)
         out = torch.full((n, 4), 77, dtype=torch.int32, device=dev)
         cnt = torch.tensor([count], dtype=torch.int32, device=dev)
@@ -261,10 +261,11 @@ def test_bvh8_knobs_do_not_change_hits(wf, dev, soup, refill, postpone, coop, ba
     rays = random_rays(np.random.default_rng(12), 60000)
     ref = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays)
     ref_any = gpu_trace(wf, dev, sc, wf.BVH2_FP32, rays, closest=False)
-    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch", "trace.bvh8.steps")
+    keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch", "trace.bvh8.steps",
+            "trace.bvh8.any_batch", "trace.bvh8.any_steps")
     old = [wf.api.tune_get(k) for k in keys]
     try:
-        for k, v in zip(keys, (refill, postpone, coop, batch, steps)):
+        for k, v in zip(keys, (refill, postpone, coop, batch, steps, batch, steps)):
             wf.api.tune_set(k, v)
         assert np.array_equal(gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays), ref)
         a8 = gpu_trace(wf, dev, sc, wf.BVH8_Q8, rays, closest=False)

@@ -47,7 +47,9 @@ def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[i
     res_c = torch.empty((closest_rays.shape[0], 4), dtype=torch.int32, device=dev)
     res_a = torch.empty((any_rays.shape[0], 4), dtype=torch.int32, device=dev)
     keys = ("trace.bvh8.refill", "trace.bvh8.postpone", "trace.bvh8.coop", "trace.bvh8.batch", "trace.bvh8.steps")
+    kind_keys = ("trace.bvh8.any_batch", "trace.bvh8.any_steps")
     old = [api.tune_get(k) for k in keys]
+    old_any = [api.tune_get(k) for k in kind_keys]
     grid = []
     for coop in coops:
         for refill in refills:
@@ -60,6 +62,8 @@ def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[i
         for setting in grid:
             for k, v in zip(keys, setting):
                 api.tune_set(k, v)
+            for k, v in zip(kind_keys, setting[3:]):  # both kinds of rays take the setting's batch and steps
+                api.tune_set(k, v)
             mc = _timeit(lambda: api.trace(scene, L.BVH8_Q8, closest_rays, res_c, closest_hit=True), reps)
             ma = _timeit(lambda: api.trace(scene, L.BVH8_Q8, any_rays, res_a, closest_hit=False), reps)
             refill, post, coop, batch, stp = setting
@@ -68,12 +72,22 @@ def tune_traversal(scene: api.Scene, closest_rays, any_rays, refills: Iterable[i
     finally:
         for k, v in zip(keys, old):
             api.tune_set(k, v)
-    # The knobs are shared by both kinds of rays: weigh them by ray count.
+        for k, v in zip(kind_keys, old_any):
+            api.tune_set(k, v)
+    # Refill, postpone and coop are shared by both kinds of rays (the best
+    # sum of both times); batch and steps are set per kind, each from the
+    # best time of its own kind among the settings with the shared knobs
+    # chosen.
     nc, na = closest_rays.shape[0], any_rays.shape[0]
     best = min(table, key=lambda e: e["closest_ms"] + e["any_ms"])
-    return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "batch": best["batch"],
-            "steps": best["steps"], "table": table, "best_closest_mrays_s": nc / (best["closest_ms"] * 1e-3) / 1e6,
-            "best_any_mrays_s": na / (best["any_ms"] * 1e-3) / 1e6}
+    same = [e for e in table if (e["refill"], e["postpone"], e["coop"]) == (best["refill"], best["postpone"],
+                                                                             best["coop"])]
+    best_c = min(same, key=lambda e: e["closest_ms"])
+    best_a = min(same, key=lambda e: e["any_ms"])
+    return {"refill": best["refill"], "postpone": best["postpone"], "coop": best["coop"], "batch": best_c["batch"],
+            "steps": best_c["steps"], "any_batch": best_a["batch"], "any_steps": best_a["steps"], "table": table,
+            "best_closest_mrays_s": nc / (best_c["closest_ms"] * 1e-3) / 1e6,
+            "best_any_mrays_s": na / (best_a["any_ms"] * 1e-3) / 1e6}
 
 
 KEY_CHOICES = ((L.MORTON_AILA32, 32), (L.MORTON_6D48, 48), (L.MORTON_6D64, 63))
@@ -261,3 +275,7 @@ def apply(traversal: Dict) -> None:
         api.tune_set("trace.bvh8.batch", traversal["batch"])
     if "steps" in traversal:
         api.tune_set("trace.bvh8.steps", traversal["steps"])
+    if "any_batch" in traversal:
+        api.tune_set("trace.bvh8.any_batch", traversal["any_batch"])
+    if "any_steps" in traversal:
+        api.tune_set("trace.bvh8.any_steps", traversal["any_steps"])

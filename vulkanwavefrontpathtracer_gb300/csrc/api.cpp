@@ -99,14 +99,14 @@ wfpt_status wfpt_tune_set(const char* key, int64_t value) {
         wfpt::set_trace_postpone((uint32_t)value);
         return WFPT_OK;
     }
-    if (k == "trace.bvh8.batch") {
-        if (value < 1 || value > 32) return invalid("trace.bvh8.batch must be in [1, 32]");
-        wfpt::set_trace_batch((uint32_t)value);
+    if (k == "trace.bvh8.batch" || k == "trace.bvh8.any_batch") {
+        if (value < 1 || value > 32) return invalid((k + " must be in [1, 32]").c_str());
+        wfpt::set_trace_batch((uint32_t)value, k == "trace.bvh8.batch");
         return WFPT_OK;
     }
-    if (k == "trace.bvh8.steps") {
-        if (value < 1 || value > 8) return invalid("trace.bvh8.steps must be in [1, 8]");
-        wfpt::set_trace_steps((uint32_t)value);
+    if (k == "trace.bvh8.steps" || k == "trace.bvh8.any_steps") {
+        if (value < 1 || value > 8) return invalid((k + " must be in [1, 8]").c_str());
+        wfpt::set_trace_steps((uint32_t)value, k == "trace.bvh8.steps");
         return WFPT_OK;
     }
     if (k == "trace.bvh8.coop") {
@@ -177,12 +177,12 @@ wfpt_status wfpt_tune_get(const char* key, int64_t* value) {
         *value = wfpt::get_trace_postpone();
         return WFPT_OK;
     }
-    if (k == "trace.bvh8.batch") {
-        *value = (int64_t)wfpt::get_trace_batch();
+    if (k == "trace.bvh8.batch" || k == "trace.bvh8.any_batch") {
+        *value = (int64_t)wfpt::get_trace_batch(k == "trace.bvh8.batch");
         return WFPT_OK;
     }
-    if (k == "trace.bvh8.steps") {
-        *value = (int64_t)wfpt::get_trace_steps();
+    if (k == "trace.bvh8.steps" || k == "trace.bvh8.any_steps") {
+        *value = (int64_t)wfpt::get_trace_steps(k == "trace.bvh8.steps");
         return WFPT_OK;
     }
     if (k == "trace.bvh8.coop") {

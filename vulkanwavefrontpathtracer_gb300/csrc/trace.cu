@@ -792,12 +792,23 @@ static uint32_t g_refill = 8;
 void set_trace_refill(uint32_t refill) { g_refill = refill < 1 ? 1 : (refill > 32 ? 32 : refill); }
 static uint32_t g_postpone = 0;
 void set_trace_postpone(uint32_t lanes) { g_postpone = lanes > 32 ? 32 : lanes; }
-static uint32_t g_batch = 16;
-static uint32_t g_steps = 2;
-void set_trace_steps(uint32_t steps) { g_steps = steps < 1 ? 1 : (steps > 8 ? 8 : steps); }
-uint32_t get_trace_steps() { return g_steps; }
-void set_trace_batch(uint32_t pairs) { g_batch = pairs < 1 ? 1 : (pairs > 32 ? 32 : pairs); }
-uint32_t get_trace_batch() { return g_batch; }
+// Cooperative-test batch and node steps per loop iteration, [0] for any-hit
+// rays, [1] for closest-hit rays.  Any-hit rays test their triangles after
+// every iteration of three node steps (a ray stops at its first hit, so
+// deferring tests only adds node steps), closest-hit rays batch 24 pairs
+// over iterations of two steps: measured on the courtyard's bounce-1 rays
+// (1.4 % / 0.6 % faster than the shared batch 16, steps 2) and its frames
+// (25.28 against 25.38 ms).
+static uint32_t g_batch[2] = {1, 24};
+static uint32_t g_steps[2] = {3, 2};
+void set_trace_steps(uint32_t steps, bool closest) {
+    g_steps[closest ? 1 : 0] = steps < 1 ? 1 : (steps > 8 ? 8 : steps);
+}
+uint32_t get_trace_steps(bool closest) { return g_steps[closest ? 1 : 0]; }
+void set_trace_batch(uint32_t pairs, bool closest) {
+    g_batch[closest ? 1 : 0] = pairs < 1 ? 1 : (pairs > 32 ? 32 : pairs);
+}
+uint32_t get_trace_batch(bool closest) { return g_batch[closest ? 1 : 0]; }
 static bool g_coop = true;
 void set_trace_coop(bool on) { g_coop = on; }
 bool get_trace_coop() { return g_coop; }
@@ -865,7 +876,7 @@ cudaError_t launch_trace(const SceneDevice& sc, int kind, const wfpt_ray* rays, 
             auto k8 = closest ? (g_count ? k_trace_bvh8_coop<true, true> : k_trace_bvh8_coop<true, false>)
                               : (g_count ? k_trace_bvh8_coop<false, true> : k_trace_bvh8_coop<false, false>);
             k8<<<pgrid, kBlock, 0, s>>>(sc.bvh8_nodes, sc.bvh8_tris, rr, out, ray_index, n, n_dev, work, g_refill,
-                                        g_batch, g_steps);
+                                        g_batch[closest ? 1 : 0], g_steps[closest ? 1 : 0]);
         } else {
             auto k8 = closest ? (g_count ? k_trace_bvh8<true, true> : k_trace_bvh8<true, false>)
                               : (g_count ? k_trace_bvh8<false, true> : k_trace_bvh8<false, false>);

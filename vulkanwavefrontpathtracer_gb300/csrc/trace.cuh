@@ -15,10 +15,12 @@ void set_trace_refill(uint32_t refill);
 // Postpone a node's triangle tests while fewer than this many lanes of the
 // warp have triangles to test (0 = never).
 void set_trace_postpone(uint32_t lanes);
-void set_trace_batch(uint32_t pairs);
-uint32_t get_trace_batch();
-void set_trace_steps(uint32_t steps);
-uint32_t get_trace_steps();
+// Cooperative triangle tests: batch size and node steps per loop iteration,
+// set separately for closest-hit and any-hit rays.
+void set_trace_batch(uint32_t pairs, bool closest);
+uint32_t get_trace_batch(bool closest);
+void set_trace_steps(uint32_t steps, bool closest);
+uint32_t get_trace_steps(bool closest);
 uint32_t get_trace_refill();
 uint32_t get_trace_postpone();
 // Warp-cooperative triangle tests in the BVH8 traversal (on by default).
