@@ -277,10 +277,17 @@ def scene_build_times(api, pos, idx, host_scene, city=None):
         cpos, cidx, hsc = city
     out["city_host_ms"] = round(hsc.info.build_ms, 1)
     hsc.close()
-    d = api.Scene(cpos, cidx, device_build=True)
-    out["city_triangles"] = int(d.info.num_triangles)
-    out["city_device_ms"] = round(d.info.build_ms, 1)
-    d.close()
+    # Three device builds, the fastest reported: a single build also times
+    # the driver mapping the first allocations of its ~1 GB of temporaries
+    # (8-50 ms seen for the same build).
+    times = []
+    for _ in range(3):
+        d = api.Scene(cpos, cidx, device_build=True)
+        out["city_triangles"] = int(d.info.num_triangles)
+        times.append(d.info.build_ms)
+        d.close()
+    out["city_device_ms"] = round(min(times), 1)
+    out["city_device_ms_all"] = [round(t, 1) for t in times]
     out["city_device_speedup"] = round(out["city_host_ms"] / max(out["city_device_ms"], 1e-3), 1)
     out["note"] = "device-built trees trace the courtyard's bounce-1 rays 10-13 % slower (PLOC vs binned SAH)"
     return out
