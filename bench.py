@@ -393,13 +393,14 @@ def run_ours(args):
     hbm, peak_kind = peaks()
     out = None
     builds = city_line = None
-    sort_big = batched = None
+    sort_big = reorder_big = batched = None
     if rank == 0:
         city_line, city = city_bounce(wf, api, dev, stream)
         builds = scene_build_times(api, pos, idx, scene, city=city)
         del city
         torch.cuda.empty_cache()
         sort_big = sort_row(api, dev, stream)
+        reorder_big = reorder_row(api, dev, stream)
         batched = batched_serving(api, dev, stream, steps=3, warmup=1)
     if rank == 0:
         cpu = cpu_baseline(args, wf, api, scene, pos, nrm, idx) if world == 1 and not args.no_cpu else None
@@ -467,6 +468,7 @@ def run_ours(args):
             "per_bounce": micro["per_bounce"],
             "per_bounce_city": city_line,
             "sort_2p26": sort_big,
+            "reorder_2p24": reorder_big,
             "batched": batched,
             "sort_reorder": {"sort_gbs": round(srt["gbs"], 1), "sort_frac": round(srt["gbs"] / hbm, 3),
                              "reorder_gbs": round(micro["reorder"]["gbs"], 1),
@@ -997,6 +999,51 @@ def sort_row(api, dev, stream, n=1 << 26, reps=5):
         del src, keys, vals, scratch
         torch.cuda.empty_cache()
     return out
+
+
+def reorder_row(api, dev, stream, n=1 << 24, reps=5):
+    """The reorder gather beyond L2: n random-order rays gathered by the
+    permutation that sorts them (32-byte records with the slot maps, 80 B
+    per ray; and 48-byte records, 112 B per ray), algorithmic GB/s against
+    the measured HBM peak."""
+    import torch
+    hbm, _ = peaks()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(n)
+    perm = torch.randperm(n, generator=gen, device=dev).to(torch.int32)
+    rays = torch.rand((n, 8), generator=gen, device=dev)
+    out = torch.empty_like(rays)
+    s2i = torch.arange(n, dtype=torch.int32, device=dev)
+    os2i = torch.empty(n, dtype=torch.int32, device=dev)
+    oi2s = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    res = {"rays": n}
+    ms = timed(lambda: api.reorder(perm, rays, out, s2i, os2i, oi2s))
+    res["ray32"] = {"ms": round(ms, 4), "gbs": round(80.0 * n / (ms * 1e-3) / 1e9, 1),
+                    "frac": round(80.0 * n / (ms * 1e-3) / 1e9 / hbm, 3), "alg_bytes_per_ray": 80}
+    del out
+    wide = torch.cat([rays, rays[:, :4]], dim=1).contiguous()
+    wide_out = torch.empty_like(wide)
+    ms = timed(lambda: api.reorder_records(perm, wide, wide_out, s2i, os2i, oi2s))
+    res["rec48"] = {"ms": round(ms, 4), "gbs": round(112.0 * n / (ms * 1e-3) / 1e9, 1),
+                    "frac": round(112.0 * n / (ms * 1e-3) / 1e9 / hbm, 3), "alg_bytes_per_ray": 112}
+    res["note"] = ("random 32/48-byte record gathers and 4-byte slot-map accesses: about 3.7x the algorithmic "
+                   "bytes reach DRAM (sector and burst granularity), the kernel's ceiling beyond L2")
+    del rays, wide, wide_out, perm, s2i, os2i, oi2s
+    torch.cuda.empty_cache()
+    return res
 
 
 def run_sort_micro(args):
