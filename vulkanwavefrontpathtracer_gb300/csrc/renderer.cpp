@@ -9,6 +9,9 @@
 //    so a frame issues no host readback (the reference reads the path count
 //    and the hit count back after every pass, RayGen.cpp:178-183 and
 //    Renderer.cpp:85-88);
+//  - the per-pass hit count (countRayHits) is taken by the reconstructSmooth
+//    kernel that reads the same hit records just before the shadow pass,
+//    instead of a separate kernel on the frame's critical stream;
 //  - buffers are sized once per resolution (capacity = width*height rays per
 //    wavefront) and the frame can be captured into one CUDA graph;
 //  - ray statistics are read back once, after the frame.
@@ -512,7 +515,7 @@ struct wfpt_renderer {
     //    slot's buffers are reused only after its previous batch is done.
     //  - Sequential: every batch on s, in the reference's order.
     cudaError_t shadow_pass(const wfpt_ray* in_rays, const wfpt_hit* in_res, const int32_t* in_s2i, uint32_t n_in,
-                            const uint32_t* n_in_dev, float* in_pixels, float* out_pixels, uint32_t* hit_counter,
+                            const uint32_t* n_in_dev, float* in_pixels, float* out_pixels,
                             uint32_t* batch_counters, cudaStream_t s, int kind, int slot_log) {
         const int S = cfg.num_shadow_samples;
         const uint32_t batch_diff = (uint32_t)(kMaxBatch / S);
@@ -555,7 +558,7 @@ struct wfpt_renderer {
             }
             pending_slots = used;
             last_slots = std::max(last_slots, used);
-            return wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, s);
+            return cudaSuccess;
         }
         uint32_t bb = 0;
         do {
@@ -584,12 +587,14 @@ struct wfpt_renderer {
             bb = be;
         } while (bb != n_in);
         last_slots = std::max(last_slots, 1);
-        return wfpt::launch_count_hits(in_res, n_in, n_in_dev, hit_counter, s);
+        return cudaSuccess;
     }
 
     // Renderer::primaryPass (Renderer.cpp:124-131).
+    // hit_counter (nullable): receives the number of primary hits (the
+    // shadow pass's input count, countRayHits) from reconstructSmooth.
     cudaError_t primary_pass(const float* s2w, const float* eye, float zfar, int pass, float* target, cudaStream_t s,
-                             const wfpt::FrameParams* fp) {
+                             const wfpt::FrameParams* fp, uint32_t* hit_counter) {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
         int sample_index = pass + cfg.num_primary_samples * (frame_index - 1);
@@ -609,7 +614,7 @@ struct wfpt_renderer {
         if ((e = wfpt::launch_fill_u32(decreases.p, one_bits, (size_t)n * 4, s)) != cudaSuccess) return e;
         return wfpt::launch_reconstruct_smooth(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(),
                                                target, decreases.as<float>(), geoms, light, bg, n, nullptr,
-                                               cfg.num_primary_samples, s);
+                                               cfg.num_primary_samples, s, hit_counter);
     }
 
     // One frame.  fp (nullable): device-side frame parameters that replace
@@ -634,7 +639,7 @@ struct wfpt_renderer {
             if ((e = wfpt::launch_init_seeds(seeds.as<uint32_t>(), n, frame_index, s, fp)) != cudaSuccess) return e;
         for (int pass = 0; pass < cfg.num_primary_samples; ++pass) {
             if (rt == WFPT_PRIMARY_RAYS) {
-                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp)) != cudaSuccess) return e;
+                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp, nullptr)) != cudaSuccess) return e;
                 continue;
             }
             // renderShadow / renderPath (Renderer.cpp:168-199).  Colour
@@ -644,10 +649,10 @@ struct wfpt_renderer {
             int ai = 0;
             if ((e = join_shadow(s)) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
-            if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp)) != cudaSuccess) return e;
+            if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp, cnt(pass, kCntHits + 0))) != cudaSuccess)
+                return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
-                                 auxb[ai], frame_pixels, cnt(pass, kCntHits + 0), cnt(pass, kCntBatch), s,
-                                 primary_kind(), 0)) != cudaSuccess)
+                                 auxb[ai], frame_pixels, cnt(pass, kCntBatch), s, primary_kind(), 0)) != cudaSuccess)
                 return e;
             if (rt != WFPT_PATH_RAYS) continue;
             int qsel = 0;  // PathQueue::swapBuffers
@@ -687,11 +692,12 @@ struct wfpt_renderer {
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
                                                          auxb[ai], decreases.as<float>(), geoms, light, bg, n,
-                                                         out_cnt, cfg.num_primary_samples, s)) != cudaSuccess)
+                                                         out_cnt, cfg.num_primary_samples, s,
+                                                         cnt(pass, kCntHits + bounce + 1))) != cudaSuccess)
                     return e;
                 if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
-                                     auxb[ai], frame_pixels, cnt(pass, kCntHits + bounce + 1),
-                                     cnt(pass, kCntBatch), s, cfg.bvh_kind, bounce + 1)) != cudaSuccess)
+                                     auxb[ai], frame_pixels, cnt(pass, kCntBatch), s, cfg.bvh_kind, bounce + 1)) !=
+                    cudaSuccess)
                     return e;
                 qsel ^= 1;  // PathQueue::swap
             }

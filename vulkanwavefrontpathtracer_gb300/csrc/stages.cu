@@ -393,15 +393,31 @@ __global__ void k_raygen_path(uint32_t* __restrict__ seeds, const wfpt_geometry*
 }
 
 // ---------------------------------------------------- reconstructSmooth
-// reconstructSmooth.comp:44-94.
+// reconstructSmooth.comp:44-94.  hit_count (nullable): also adds the
+// number of hit records among the n rays to *hit_count, the count
+// countRayHits.comp takes for the shadow pass that follows (same rays, same
+// results), one atomic per block.
 __global__ void k_reconstruct_smooth(const float4* __restrict__ rays, const int4* __restrict__ results,
                                      const int32_t* __restrict__ i2p, float4* __restrict__ pixels,
                                      const float4* __restrict__ decreases,
                                      const wfpt_geometry* __restrict__ geoms, float lx, float ly,
                                      float lz, float bx, float by, float bz, uint32_t n,
-                                     const uint32_t* __restrict__ n_dev, int spp) {
+                                     const uint32_t* __restrict__ n_dev, int spp,
+                                     uint32_t* __restrict__ hit_count) {
     uint32_t task = blockIdx.x * blockDim.x + threadIdx.x;
-    if (task >= load_count(n, n_dev)) return;
+    const bool valid = task < load_count(n, n_dev);
+    if (hit_count != nullptr) {
+        __shared__ uint32_t s_w[kBlock / 32];
+        const uint32_t c = __popc(__ballot_sync(0xffffffffu, valid && results[task].x >= 0));
+        if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < kBlock / 32; ++w) t += s_w[w];
+            if (t) atomicAdd(hit_count, t);
+        }
+    }
+    if (!valid) return;
     int pixel = i2p[task];
     float4 pc = pixels[pixel];
     f3 color = mk(pc.x, pc.y, pc.z);
@@ -770,12 +786,12 @@ cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geom
 cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res, const int32_t* i2p,
                                       float* pixels, const float* decreases, const wfpt_geometry* geoms,
                                       const float* light, const float* bg, uint32_t n,
-                                      const uint32_t* n_dev, int spp, cudaStream_t s) {
+                                      const uint32_t* n_dev, int spp, cudaStream_t s, uint32_t* hit_count) {
     if (n == 0) return cudaSuccess;
     k_reconstruct_smooth<<<grid_for(n), kBlock, 0, s>>>(
         reinterpret_cast<const float4*>(rays), reinterpret_cast<const int4*>(res), i2p,
         reinterpret_cast<float4*>(pixels), reinterpret_cast<const float4*>(decreases), geoms, light[0],
-        light[1], light[2], bg[0], bg[1], bg[2], n, n_dev, spp);
+        light[1], light[2], bg[0], bg[1], bg[2], n, n_dev, spp, hit_count);
     count_launch();
     return cudaGetLastError();
 }

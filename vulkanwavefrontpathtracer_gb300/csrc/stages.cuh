@@ -56,7 +56,8 @@ cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geom
 cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res, const int32_t* i2p,
                                       float* pixels, const float* decreases, const wfpt_geometry* geoms,
                                       const float* light, const float* bg, uint32_t n,
-                                      const uint32_t* n_dev, int spp, cudaStream_t s);
+                                      const uint32_t* n_dev, int spp, cudaStream_t s,
+                                      uint32_t* hit_count = nullptr);
 cudaError_t launch_reconstruct_shadow(const wfpt_hit* res, const int32_t* i2p, const int32_t* i2s,
                                       const float* in_pixels, float* out_pixels, int bb, int bs,
                                       const uint32_t* n_in_dev, int S, int replace, cudaStream_t s);
