@@ -593,8 +593,11 @@ struct wfpt_renderer {
     // Renderer::primaryPass (Renderer.cpp:124-131).
     // hit_counter (nullable): receives the number of primary hits (the
     // shadow pass's input count, countRayHits) from reconstructSmooth.
+    // fresh: target is this pass's colour buffer, taken as cleared (its
+    // pixels are written, not accumulated); otherwise reconstructSmooth adds
+    // into it (the frame buffer of the primary-rays mode, over the samples).
     cudaError_t primary_pass(const float* s2w, const float* eye, float zfar, int pass, float* target, cudaStream_t s,
-                             const wfpt::FrameParams* fp, uint32_t* hit_counter) {
+                             const wfpt::FrameParams* fp, uint32_t* hit_counter, bool fresh) {
         uint32_t n = (uint32_t)width * height;
         cudaError_t e;
         int sample_index = pass + cfg.num_primary_samples * (frame_index - 1);
@@ -614,7 +617,7 @@ struct wfpt_renderer {
         if ((e = wfpt::launch_fill_u32(decreases.p, one_bits, (size_t)n * 4, s)) != cudaSuccess) return e;
         return wfpt::launch_reconstruct_smooth(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(),
                                                target, decreases.as<float>(), geoms, light, bg, n, nullptr,
-                                               cfg.num_primary_samples, s, hit_counter);
+                                               cfg.num_primary_samples, s, hit_counter, fresh);
     }
 
     // One frame.  fp (nullable): device-side frame parameters that replace
@@ -639,7 +642,8 @@ struct wfpt_renderer {
             if ((e = wfpt::launch_init_seeds(seeds.as<uint32_t>(), n, frame_index, s, fp)) != cudaSuccess) return e;
         for (int pass = 0; pass < cfg.num_primary_samples; ++pass) {
             if (rt == WFPT_PRIMARY_RAYS) {
-                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp, nullptr)) != cudaSuccess) return e;
+                if ((e = primary_pass(s2w, eye, zfar, pass, frame_pixels, s, fp, nullptr, false)) != cudaSuccess)
+                    return e;
                 continue;
             }
             // renderShadow / renderPath (Renderer.cpp:168-199).  Colour
@@ -648,8 +652,11 @@ struct wfpt_renderer {
             float* auxb[2] = {aux.as<float>(), cfg.shadow_overlap ? aux2.as<float>() : aux.as<float>()};
             int ai = 0;
             if ((e = join_shadow(s)) != cudaSuccess) return e;
-            if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
-            if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp, cnt(pass, kCntHits + 0))) != cudaSuccess)
+            // The colour buffers are not cleared (Renderer.cpp clears them per
+            // pass): every pixel the shadow pass reads back was written by
+            // this pass's reconstructSmooth in fresh mode.
+            if ((e = primary_pass(s2w, eye, zfar, pass, auxb[ai], s, fp, cnt(pass, kCntHits + 0), true)) !=
+                cudaSuccess)
                 return e;
             if ((e = shadow_pass(primary.rays_cur(), primary.results.as<wfpt_hit>(), i2p.as<int32_t>(), n, nullptr,
                                  auxb[ai], frame_pixels, cnt(pass, kCntBatch), s, primary_kind(), 0)) != cudaSuccess)
@@ -658,7 +665,6 @@ struct wfpt_renderer {
             int qsel = 0;  // PathQueue::swapBuffers
             for (int bounce = 0; bounce < cfg.recursion_depth; ++bounce) {
                 ai ^= 1;
-                if ((e = cudaMemsetAsync(auxb[ai], 0, (size_t)n * 16, s)) != cudaSuccess) return e;
                 RayBufferDev& out = queue[qsel ? 0 : 1];
                 const wfpt_ray* in_rays;
                 const wfpt_hit* in_res;
@@ -693,7 +699,7 @@ struct wfpt_renderer {
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
                                                          auxb[ai], decreases.as<float>(), geoms, light, bg, n,
                                                          out_cnt, cfg.num_primary_samples, s,
-                                                         cnt(pass, kCntHits + bounce + 1))) != cudaSuccess)
+                                                         cnt(pass, kCntHits + bounce + 1), true)) != cudaSuccess)
                     return e;
                 if ((e = shadow_pass(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(), n, out_cnt,
                                      auxb[ai], frame_pixels, cnt(pass, kCntBatch), s, cfg.bvh_kind, bounce + 1)) !=

@@ -396,14 +396,17 @@ __global__ void k_raygen_path(uint32_t* __restrict__ seeds, const wfpt_geometry*
 // reconstructSmooth.comp:44-94.  hit_count (nullable): also adds the
 // number of hit records among the n rays to *hit_count, the count
 // countRayHits.comp takes for the shadow pass that follows (same rays, same
-// results), one atomic per block.
+// results), one atomic per block.  fresh != 0: the pixels of these rays
+// are taken as zero instead of being read (the renderer's per-pass colour
+// buffer, cleared before every pass in the reference: each of its pixels
+// has one ray per pass), with the same addition to zero.
 __global__ void k_reconstruct_smooth(const float4* __restrict__ rays, const int4* __restrict__ results,
                                      const int32_t* __restrict__ i2p, float4* __restrict__ pixels,
                                      const float4* __restrict__ decreases,
                                      const wfpt_geometry* __restrict__ geoms, float lx, float ly,
                                      float lz, float bx, float by, float bz, uint32_t n,
                                      const uint32_t* __restrict__ n_dev, int spp,
-                                     uint32_t* __restrict__ hit_count) {
+                                     uint32_t* __restrict__ hit_count, int fresh) {
     uint32_t task = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = task < load_count(n, n_dev);
     if (hit_count != nullptr) {
@@ -419,7 +422,7 @@ __global__ void k_reconstruct_smooth(const float4* __restrict__ rays, const int4
     }
     if (!valid) return;
     int pixel = i2p[task];
-    float4 pc = pixels[pixel];
+    const float4 pc = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : pixels[pixel];
     f3 color = mk(pc.x, pc.y, pc.z);
     float4 dc = decreases[pixel];
     f3 dec = mk(dc.x, dc.y, dc.z);
@@ -786,12 +789,13 @@ cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geom
 cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res, const int32_t* i2p,
                                       float* pixels, const float* decreases, const wfpt_geometry* geoms,
                                       const float* light, const float* bg, uint32_t n,
-                                      const uint32_t* n_dev, int spp, cudaStream_t s, uint32_t* hit_count) {
+                                      const uint32_t* n_dev, int spp, cudaStream_t s, uint32_t* hit_count,
+                                      bool fresh) {
     if (n == 0) return cudaSuccess;
     k_reconstruct_smooth<<<grid_for(n), kBlock, 0, s>>>(
         reinterpret_cast<const float4*>(rays), reinterpret_cast<const int4*>(res), i2p,
         reinterpret_cast<float4*>(pixels), reinterpret_cast<const float4*>(decreases), geoms, light[0],
-        light[1], light[2], bg[0], bg[1], bg[2], n, n_dev, spp, hit_count);
+        light[1], light[2], bg[0], bg[1], bg[2], n, n_dev, spp, hit_count, fresh ? 1 : 0);
     count_launch();
     return cudaGetLastError();
 }

@@ -57,7 +57,7 @@ cudaError_t launch_reconstruct_smooth(const wfpt_ray* rays, const wfpt_hit* res,
                                       float* pixels, const float* decreases, const wfpt_geometry* geoms,
                                       const float* light, const float* bg, uint32_t n,
                                       const uint32_t* n_dev, int spp, cudaStream_t s,
-                                      uint32_t* hit_count = nullptr);
+                                      uint32_t* hit_count = nullptr, bool fresh = false);
 cudaError_t launch_reconstruct_shadow(const wfpt_hit* res, const int32_t* i2p, const int32_t* i2s,
                                       const float* in_pixels, float* out_pixels, int bb, int bs,
                                       const uint32_t* n_in_dev, int S, int replace, cudaStream_t s);
