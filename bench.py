@@ -662,6 +662,26 @@ def run_trace_profile(args):
     torch.cuda.synchronize()
     print(json.dumps({"trace_profile": "city" if args.city else "courtyard", "resolution": [w, h],
                       "path_rays": m, "shadow_rays": S * m}))
+    if args.trace_counts:
+        # The same five launches through the counting kernels: node visits,
+        # triangle tests and (BVH8) persistent-warp loop iterations per ray.
+        forms = (("bvh2 closest", wf.BVH2_FP32, path, res, True), ("bvh8 closest unsorted", wf.BVH8_Q8, path, res, True),
+                 ("bvh8 closest sorted", wf.BVH8_Q8, srt, res, True), ("bvh8 any", wf.BVH8_Q8, srays, sres, False),
+                 ("bvh2 any", wf.BVH2_FP32, srays, sres, False))
+        old = api.tune_get("trace.count")
+        api.tune_set("trace.count", 1)
+        try:
+            for label, kind, rays, out, closest in forms:
+                api.trace_counters(reset=True)
+                api.trace(scene, kind, rays, out, closest_hit=closest)
+                torch.cuda.synchronize()
+                c = api.trace_counters(reset=True)
+                nr = rays.shape[0]
+                print(json.dumps({"form": label, "rays": nr, "hit_fraction": round(float((out[:nr, 0] >= 0).float().mean()), 3),
+                                  "nodes_per_ray": round(c["nodes"] / nr, 2), "tris_per_ray": round(c["tris"] / nr, 2),
+                                  "warp_iters_per_32_rays": round(c["warp_iters"] * 32 / nr, 2)}))
+        finally:
+            api.tune_set("trace.count", old)
 
 
 def run_sweep(args):
@@ -1174,6 +1194,8 @@ def main():
     ap.add_argument("--batched", action="store_true", help="the 64-request batched serving workload")
     ap.add_argument("--trace-profile", action="store_true",
                     help="each traversal form launched once on a small bounce-1 case (for kernel profiles)")
+    ap.add_argument("--trace-counts", action="store_true",
+                    help="with --trace-profile: node visits and triangle tests per ray of each form (counting kernels)")
     ap.add_argument("--batch-requests", type=int, default=64)
     args = ap.parse_args()
     if args.batched:
