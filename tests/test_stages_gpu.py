@@ -301,6 +301,35 @@ def test_reorder_full_size_properties(wf, dev):
     assert torch.equal(oi2s[os2i.to(torch.int64)], slots)
 
 
+@pytest.mark.parametrize("words,counted", [(12, False), (4, True), (16, False)])
+def test_reorder_records_beyond_l2(wf, dev, words, counted):
+    """Record gathers past the size from which the kernels stream the
+    records with an L2 evict-first policy (4,194,304 rays): 48-, 16- and
+    64-byte records by a random permutation, with slot maps; `counted`
+    reads the ray count from device memory (the policy follows the host
+    capacity)."""
+    import torch
+    n = (1 << 22) + 4099
+    g = torch.Generator(device=dev)
+    g.manual_seed(words)
+    recs = torch.randint(-2**31, 2**31 - 1, (n, words), generator=g, device=dev, dtype=torch.int32)
+    idx = torch.randperm(n, generator=g, device=dev).to(torch.int32)
+    s2i = torch.randperm(n, generator=g, device=dev).to(torch.int32)
+    out = torch.full((n, words), -7, dtype=torch.int32, device=dev)
+    os2i = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    oi2s = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    m = n - 1000 if counted else n
+    n_dev = torch.tensor([m], dtype=torch.int32, device=dev) if counted else None
+    wf.api.reorder_records(idx, recs, out, s2i, os2i, oi2s, n=n, n_dev=n_dev)
+    torch.cuda.synchronize()
+    assert wf.api.device_status() == 0
+    li = idx[:m].to(torch.int64)
+    assert torch.equal(out[:m], recs[li]) and bool((out[m:] == -7).all())
+    assert torch.equal(os2i[:m], s2i[li]) and bool((os2i[m:] == -7).all())
+    written = os2i[:m].to(torch.int64)
+    assert torch.equal(oi2s[written], torch.arange(m, dtype=torch.int32, device=dev))
+
+
 def test_interpolate_colors_fp64_matches_oracle(wf, orc, dev):
     """The FP64 running mean over five frames, bit-exact against the
     oracle's double evaluation (pixels, tone-mapped frame and the double

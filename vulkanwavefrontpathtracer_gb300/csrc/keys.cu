@@ -101,20 +101,63 @@ __global__ void k_morton(const float4* __restrict__ rays, uint32_t n, const uint
     indices[i] = i;
 }
 
+// Gathers beyond L2 (STREAM): the index, the gathered records and the
+// written records are touched once, so they are loaded and stored with an
+// L2 evict-first policy, and the L2 keeps the randomly accessed 4-byte slot
+// map entries (each 32-byte sector of them is touched eight times, at random
+// moments) for longer.  Random-permutation gathers of 32- / 48-byte records:
+// 7 / 10 % faster at 2^22 rays, 26 / 20 % at 2^23, 9 / 6 % at 2^24, 2 % at
+// 2^25; an evict-last policy on the slot maps instead was 3-12 % slower.
+// Smaller gathers (a frame's 2.07M-ray wavefront, whose records the next
+// kernel reads back from L2) keep plain accesses: the policy made 2^21 rays
+// 5-10 % slower.
+constexpr uint32_t kStreamRecords = 1u << 22;
+
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+template <bool STREAM>
+__device__ __forceinline__ uint4 load_record(const uint4* p, uint64_t pol) {
+    if (!STREAM) return __ldg(p);
+    uint4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+template <bool STREAM>
+__device__ __forceinline__ void store_record(uint4* p, uint4 v, uint64_t pol) {
+    if (!STREAM) {
+        *p = v;
+        return;
+    }
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w), "l"(pol)
+                 : "memory");
+}
+
 // reorderRays.comp:37-45.
-__global__ void k_reorder(const uint32_t* __restrict__ idx, const float4* __restrict__ in_rays,
-                          float4* __restrict__ out_rays, const int32_t* __restrict__ in_s2i,
+template <bool STREAM>
+__global__ void k_reorder(const uint32_t* __restrict__ idx, const uint4* __restrict__ in_rays,
+                          uint4* __restrict__ out_rays, const int32_t* __restrict__ in_s2i,
                           int32_t* __restrict__ out_s2i, int32_t* __restrict__ out_i2s, uint32_t n,
                           const uint32_t* __restrict__ n_dev) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= load_count(n, n_dev)) return;
-    uint32_t old = idx[i];
+    const uint64_t pol = STREAM ? l2_evict_first_policy() : 0u;
+    uint32_t old = STREAM ? __ldcs(idx + i) : idx[i];
     int32_t index = in_s2i[old];
-    float4 a = in_rays[2 * old + 0];
-    float4 b = in_rays[2 * old + 1];
-    out_rays[2 * i + 0] = a;
-    out_rays[2 * i + 1] = b;
-    out_s2i[i] = index;
+    uint4 a = load_record<STREAM>(in_rays + 2 * (size_t)old + 0, pol);
+    uint4 b = load_record<STREAM>(in_rays + 2 * (size_t)old + 1, pol);
+    store_record<STREAM>(out_rays + 2 * (size_t)i + 0, a, pol);
+    store_record<STREAM>(out_rays + 2 * (size_t)i + 1, b, pol);
+    if (STREAM) {
+        __stcs(out_s2i + i, index);
+    } else {
+        out_s2i[i] = index;
+    }
     out_i2s[index] = (int32_t)i;
 }
 
@@ -122,22 +165,27 @@ __global__ void k_reorder(const uint32_t* __restrict__ idx, const float4* __rest
 // 48 B = 3 chunks).  One thread per record: the C 16-byte loads of a record
 // are issued together; stores are coalesced across the warp.  The slot maps
 // are optional (in_s2i == nullptr: plain gather).
-template <int C>
+template <int C, bool STREAM>
 __global__ void k_reorder_records(const uint32_t* __restrict__ idx, const uint4* __restrict__ in_rec,
                                   uint4* __restrict__ out_rec, const int32_t* __restrict__ in_s2i,
                                   int32_t* __restrict__ out_s2i, int32_t* __restrict__ out_i2s, uint32_t n,
                                   const uint32_t* __restrict__ n_dev) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= load_count(n, n_dev)) return;
-    uint32_t old = idx[i];
+    const uint64_t pol = STREAM ? l2_evict_first_policy() : 0u;
+    uint32_t old = STREAM ? __ldcs(idx + i) : idx[i];
     uint4 v[C];
 #pragma unroll
-    for (int c = 0; c < C; ++c) v[c] = __ldg(in_rec + (size_t)C * old + c);
+    for (int c = 0; c < C; ++c) v[c] = load_record<STREAM>(in_rec + (size_t)C * old + c, pol);
 #pragma unroll
-    for (int c = 0; c < C; ++c) out_rec[(size_t)C * i + c] = v[c];
+    for (int c = 0; c < C; ++c) store_record<STREAM>(out_rec + (size_t)C * i + c, v[c], pol);
     if (in_s2i != nullptr) {
         int32_t index = in_s2i[old];
-        out_s2i[i] = index;
+        if (STREAM) {
+            __stcs(out_s2i + i, index);
+        } else {
+            out_s2i[i] = index;
+        }
         out_i2s[index] = (int32_t)i;
     }
 }
@@ -166,8 +214,9 @@ cudaError_t launch_reorder(const uint32_t* idx, const wfpt_ray* in_rays, wfpt_ra
                            const uint32_t* n_dev, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     unsigned grid = (n + kBlock - 1) / kBlock;
-    k_reorder<<<grid, kBlock, 0, s>>>(idx, reinterpret_cast<const float4*>(in_rays),
-                                      reinterpret_cast<float4*>(out_rays), in_s2i, out_s2i, out_i2s, n, n_dev);
+    auto k = n >= kStreamRecords ? k_reorder<true> : k_reorder<false>;
+    k<<<grid, kBlock, 0, s>>>(idx, reinterpret_cast<const uint4*>(in_rays), reinterpret_cast<uint4*>(out_rays), in_s2i,
+                              out_s2i, out_i2s, n, n_dev);
     count_launch();
     return cudaGetLastError();
 }
@@ -179,11 +228,15 @@ cudaError_t launch_reorder_records(const uint32_t* idx, const void* in_records, 
     unsigned grid = (n + kBlock - 1) / kBlock;
     const uint4* in = static_cast<const uint4*>(in_records);
     uint4* out = static_cast<uint4*>(out_records);
+    const bool st = n >= kStreamRecords;
     switch (record_bytes) {
-        case 16: k_reorder_records<1><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
-        case 32: k_reorder_records<2><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
-        case 48: k_reorder_records<3><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
-        case 64: k_reorder_records<4><<<grid, kBlock, 0, s>>>(idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev); break;
+#define WFPT_REORDER_REC(B, C)                                                                                       \
+    case B:                                                                                                          \
+        (st ? k_reorder_records<C, true> : k_reorder_records<C, false>)<<<grid, kBlock, 0, s>>>(                     \
+            idx, in, out, in_s2i, out_s2i, out_i2s, n, n_dev);                                                       \
+        break;
+        WFPT_REORDER_REC(16, 1) WFPT_REORDER_REC(32, 2) WFPT_REORDER_REC(48, 3) WFPT_REORDER_REC(64, 4)
+#undef WFPT_REORDER_REC
         default: return cudaErrorInvalidValue;
     }
     count_launch();
