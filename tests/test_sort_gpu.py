@@ -219,6 +219,31 @@ def test_sort_unaligned_buffers(wf, dev, key_bits):
     assert wf.api.device_status() == 0
 
 
+@pytest.mark.parametrize("key_bits,n,counted", [(44, (1 << 24) + 4097, False), (64, (1 << 24) + 1, False),
+                                                (63, (1 << 24) + 77, True), (32, (1 << 24) + 3, False)])
+def test_sort_large_histogram_bit_exact(wf, dev, key_bits, n, counted):
+    """Sorts of 2^24 pairs and more with five passes or more build their
+    digit histograms in lane-private 16-bit counter columns: the stable
+    order, bit for bit, for a key width that is not a multiple of 8 (44
+    bits: 6 passes, the top one on 4 bits), full 64-bit keys, a count read
+    from device memory (the histogram's grid follows the host capacity, the
+    count the device value), and 32-bit keys (four passes: the plain
+    histogram kernel) at the same size."""
+    rng = np.random.default_rng(n + key_bits)
+    if key_bits > 32:
+        keys = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
+    else:
+        keys = rng.integers(0, 2**32, n, dtype=np.uint32)
+    keys[::3] = keys[7]  # a third of the keys equal: one digit bin holds them in every pass
+    m = n - 5000 if counted else n
+    k, v = run_sort(wf, dev, keys, key_bits, n_dev=m if counted else None)
+    rk, rv = stable_ref(keys[:m], key_bits)
+    assert np.array_equal(v[:m], rv) and np.array_equal(k[:m], rk)
+    if counted:
+        assert np.array_equal(k[m:], keys[m:]) and np.array_equal(v[m:], np.arange(m, n, dtype=np.uint32))
+    assert wf.api.device_status() == 0
+
+
 @pytest.mark.parametrize("key_bits", [63, 32])
 def test_sort_full_size_properties(wf, dev, key_bits):
     """2^26 pairs, the microbenchmark's largest size (beyond what a CPU
