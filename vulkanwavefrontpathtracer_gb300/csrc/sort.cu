@@ -705,8 +705,8 @@ cudaError_t sort_selftest_timeout(cudaStream_t s) {
     constexpr uint32_t TILE = kSortThreads * KPT, N = 2 * TILE;
     cudaError_t e = sort_prepare();
     if (e != cudaSuccess) return e;
-    uint32_t* buf = nullptr;  // keys, values, keys out, values out, ticket, lookback
-    const size_t words = 4 * (size_t)N + 1 + 2 * kRadix;
+    uint32_t* buf = nullptr;  // keys, values, keys out, values out, ticket, lookback, histogram
+    const size_t words = 4 * (size_t)N + 1 + 3 * kRadix;
     if ((e = dev_malloc(reinterpret_cast<void**>(&buf), words * sizeof(uint32_t))) != cudaSuccess) return e;
     uint32_t* keys = buf;
     uint32_t* vals = keys + N;
@@ -714,13 +714,13 @@ cudaError_t sort_selftest_timeout(cudaStream_t s) {
     uint32_t* vals_out = keys_out + N;
     uint32_t* ticket = vals_out + N;
     uint32_t* lookback = ticket + 1;
+    uint32_t* hist = lookback + 2 * kRadix;  // zero: the global digit bases of an unsorted pass
     const uint32_t one = 1;
     e = cudaMemsetAsync(buf, 0, words * sizeof(uint32_t), s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ticket, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
         k_onesweep<uint32_t, KPT, 8><<<1, kSortThreads, onesweep_smem<uint32_t, KPT, 8>(), s>>>(
-            keys, vals, keys_out, vals_out, N, nullptr, 0, 0xFFu, lookback /* unused for tile 1 */, lookback,
-            ticket, 0, 0u);
+            keys, vals, keys_out, vals_out, N, nullptr, 0, 0xFFu, hist, lookback, ticket, 0, 0u);
         count_launch();
         e = cudaGetLastError();
     }

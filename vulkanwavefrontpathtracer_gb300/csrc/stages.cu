@@ -553,20 +553,20 @@ __device__ __forceinline__ double dblend(double c1, double c0, double a, double 
 }
 
 __global__ void k_interpolate_colors_fp64(float4* __restrict__ frame_pixels, float4* __restrict__ pixels,
-                                          double4* __restrict__ accum, uint32_t n, int frame_index, float key,
+                                          double4_32a* __restrict__ accum, uint32_t n, int frame_index, float key,
                                           float white, const FrameParams* __restrict__ fp) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (fp) frame_index = fp->frame_index;
     float4 p1 = frame_pixels[i];
-    double4 m;
+    double4_32a m;
     if (frame_index > 1) {
-        double4 m0 = accum[i];
+        double4_32a m0 = accum[i];
         double a = __ddiv_rn(1.0, (double)frame_index);
         double b = __dmul_rn(a, __dsub_rn((double)frame_index, 1.0));
-        m = make_double4(dblend(p1.x, m0.x, a, b), dblend(p1.y, m0.y, a, b), dblend(p1.z, m0.z, a, b), 1.0);
+        m = make_double4_32a(dblend(p1.x, m0.x, a, b), dblend(p1.y, m0.y, a, b), dblend(p1.z, m0.z, a, b), 1.0);
     } else {
-        m = make_double4(p1.x, p1.y, p1.z, 1.0);
+        m = make_double4_32a(p1.x, p1.y, p1.z, 1.0);
     }
     accum[i] = m;
     f3 c = mk(__double2float_rn(m.x), __double2float_rn(m.y), __double2float_rn(m.z));
@@ -835,7 +835,7 @@ cudaError_t launch_interpolate_colors_fp64(float* frame_pixels, float* pixels, d
     if (n == 0) return cudaSuccess;
     k_interpolate_colors_fp64<<<grid_for(n), kBlock, 0, s>>>(reinterpret_cast<float4*>(frame_pixels),
                                                              reinterpret_cast<float4*>(pixels),
-                                                             reinterpret_cast<double4*>(accum), n, frame_index, key,
+                                                             reinterpret_cast<double4_32a*>(accum), n, frame_index, key,
                                                              white, fp);
     count_launch();
     return cudaGetLastError();
