@@ -455,9 +455,11 @@ struct wfpt_renderer {
     // the sort log slot); a timed sorted pass first traces its rays
     // unsorted, for the log's trace time, as Renderer.cpp:259-264 and
     // :281-286 do (the sorted trace then overwrites those results).
+    // keys_ready: rb.keys / rb.idx already hold the rays' Morton keys (written
+    // by the path-ray generation), so the sort starts without the Morton kernel.
     cudaError_t trace_rays(RayBufferDev& rb, uint32_t n, const uint32_t* n_dev, bool sort, bool reorder, bool closest,
                            cudaStream_t s, uint32_t* wk, DevBuf& scratch, int kind, int total = T_NONE,
-                           int log = -1) {
+                           int log = -1, bool keys_ready = false) {
         const wfpt::SceneDevice& sc = *wfpt::scene_device(scene);
         cudaError_t e;
         auto plain = [&]() {
@@ -467,7 +469,7 @@ struct wfpt_renderer {
         if (!sort) return timed(s, total, C_NONE, -1, plain);
         if (timing_on && log >= 0 && (e = timed(s, T_NONE, C_TRACE, log, plain)) != cudaSuccess) return e;
         float size[3] = {smax[0] - smin[0], smax[1] - smin[1], smax[2] - smin[2]};
-        if ((e = timed(s, total, C_MORTON, log, [&]() {
+        if (!keys_ready && (e = timed(s, total, C_MORTON, log, [&]() {
                  return wfpt::launch_morton(rb.rays_cur(), n, n_dev, smin, size, cfg.morton_kind, rb.keys.p,
                                             rb.idx.as<uint32_t>(), s);
              })) != cudaSuccess)
@@ -684,17 +686,33 @@ struct wfpt_renderer {
                 }
                 out.swapped = false;
                 uint32_t* out_cnt = cnt(pass, kCntPath + bounce);
+                const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
+                // A sorted bounce gets its Morton keys from the path-ray
+                // generation (the same keys the Morton kernel would compute
+                // from the written rays); a timed frame keeps the Morton
+                // kernel, whose time the sort log reports.
+                wfpt::MortonOut mo{};
+                const bool fused_keys = sort_b && !timing_on;
+                if (fused_keys) {
+                    mo.kind = cfg.morton_kind;
+                    mo.keys = out.keys.p;
+                    mo.indices = out.idx.as<uint32_t>();
+                    for (int k = 0; k < 3; ++k) {
+                        mo.box.smin[k] = smin[k];
+                        mo.box.ssize[k] = smax[k] - smin[k];
+                    }
+                }
                 // Renderer::pathPass -> tracePathRays (Renderer.cpp:156-162, 277-297).
                 if ((e = timed(s, T_PATH, C_NONE, -1, [&]() {
                          return wfpt::launch_raygen_path(seeds.as<uint32_t>(), geoms, in_rays, out.rays_cur(), in_s2i,
                                                          out.s2i_cur(), in_res, decreases.as<float>(), out_cnt, n,
-                                                         in_cnt, cfg.albedo, path_scratch.p, s);
+                                                         in_cnt, cfg.albedo, path_scratch.p, s,
+                                                         fused_keys ? &mo : nullptr);
                      })) != cudaSuccess)
                     return e;
-                const bool sort_b = cfg.sort_path_rays != 0 && ((cfg.path_sort_skip >> bounce) & 1) == 0;
                 if ((e = trace_rays(out, n, out_cnt, sort_b, sort_b && cfg.reorder_path_rays != 0, true, s,
-                                    work.as<uint32_t>(), sort_scratch, cfg.bvh_kind, T_PATH, 100 + bounce)) !=
-                    cudaSuccess)
+                                    work.as<uint32_t>(), sort_scratch, cfg.bvh_kind, T_PATH, 100 + bounce,
+                                    fused_keys)) != cudaSuccess)
                     return e;
                 if ((e = wfpt::launch_reconstruct_smooth(out.rays_cur(), out.results.as<wfpt_hit>(), out.s2i_cur(),
                                                          auxb[ai], decreases.as<float>(), geoms, light, bg, n,

@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "morton.cuh"
 #include "stages.cuh"
 
 namespace wfpt {
@@ -309,14 +310,19 @@ __device__ uint32_t tile_prefix(uint32_t* tile_state, uint32_t tile, uint32_t co
 }
 
 // raygenPath.comp:95-167.  scratch[0] = tile ticket, scratch[1..] = tile
-// states; both zeroed by the host before the launch.
+// states; both zeroed by the host before the launch.  MK >= 0: also writes
+// the Morton key of kind MK of every output ray and its index (keys[dst],
+// key_idx[dst] = dst), which the Morton kernel would otherwise compute
+// from the written rays.
+template <int MK>
 __global__ void k_raygen_path(uint32_t* __restrict__ seeds, const wfpt_geometry* __restrict__ geoms,
                               const float4* __restrict__ in_rays, float4* __restrict__ out_rays,
                               const int32_t* __restrict__ in_i2p, int32_t* __restrict__ out_i2p,
                               const int4* __restrict__ in_results, float4* __restrict__ decreases,
                               uint32_t* __restrict__ out_count, uint32_t n,
                               const uint32_t* __restrict__ n_dev, float albedo,
-                              uint32_t* __restrict__ scratch) {
+                              uint32_t* __restrict__ scratch, void* __restrict__ keys,
+                              uint32_t* __restrict__ key_idx, Box6 box) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_warp[kBlock / 32];
     uint32_t count = load_count(n, n_dev);
@@ -383,6 +389,10 @@ __global__ void k_raygen_path(uint32_t* __restrict__ seeds, const wfpt_geometry*
         out_rays[2 * dst + 0] = o0;
         out_rays[2 * dst + 1] = o1;
         out_i2p[dst] = pixel;
+        if (MK >= 0) {
+            write_morton_key<(MK < 0 ? 0 : MK)>(keys, dst, o0, o1, box);
+            key_idx[dst] = dst;
+        }
         dc.x = __fmul_rn(dc.x, albedo);
         dc.y = __fmul_rn(dc.y, albedo);
         dc.z = __fmul_rn(dc.z, albedo);
@@ -635,15 +645,23 @@ cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, cons
                                wfpt_ray* out_rays, const int32_t* in_i2p, int32_t* out_i2p,
                                const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
                                uint32_t n, const uint32_t* n_dev, float albedo, void* scratch,
-                               cudaStream_t s) {
+                               cudaStream_t s, const MortonOut* mo) {
     size_t tiles = ((size_t)n + kBlock - 1) / kBlock;
     cudaError_t e = cudaMemsetAsync(scratch, 0, (1 + tiles) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     unsigned grid = tiles == 0 ? 1u : (unsigned)tiles;
-    k_raygen_path<<<grid, kBlock, 0, s>>>(
-        seeds, geoms, reinterpret_cast<const float4*>(in_rays), reinterpret_cast<float4*>(out_rays), in_i2p,
-        out_i2p, reinterpret_cast<const int4*>(in_res), reinterpret_cast<float4*>(decreases), out_count, n,
-        n_dev, albedo, reinterpret_cast<uint32_t*>(scratch));
+    const Box6 box = mo ? mo->box : Box6{};
+    auto k = k_raygen_path<-1>;
+    if (mo != nullptr) {
+        k = mo->kind == WFPT_MORTON_AILA32 ? k_raygen_path<WFPT_MORTON_AILA32>
+            : mo->kind == WFPT_MORTON_6D48 ? k_raygen_path<WFPT_MORTON_6D48>
+                                           : k_raygen_path<WFPT_MORTON_6D64>;
+    }
+    k<<<grid, kBlock, 0, s>>>(seeds, geoms, reinterpret_cast<const float4*>(in_rays),
+                              reinterpret_cast<float4*>(out_rays), in_i2p, out_i2p,
+                              reinterpret_cast<const int4*>(in_res), reinterpret_cast<float4*>(decreases),
+                              out_count, n, n_dev, albedo, reinterpret_cast<uint32_t*>(scratch),
+                              mo ? mo->keys : nullptr, mo ? mo->indices : nullptr, box);
     count_launch();
     return cudaGetLastError();
 }
@@ -676,8 +694,9 @@ cudaError_t raygen_path_selftest_timeout(cudaStream_t s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(results, 0xFF, N * sizeof(int4), s);  // every ray a miss
     if (e == cudaSuccess) e = cudaMemcpyAsync(scratch, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
-        k_raygen_path<<<1, kBlock, 0, s>>>(seeds, nullptr, in_rays, out_rays, in_i2p, out_i2p, results, decreases,
-                                           count, N, nullptr, 0.8f, scratch);
+        k_raygen_path<-1><<<1, kBlock, 0, s>>>(seeds, nullptr, in_rays, out_rays, in_i2p, out_i2p, results,
+                                               decreases, count, N, nullptr, 0.8f, scratch, nullptr, nullptr,
+                                               Box6{});
         count_launch();
         e = cudaGetLastError();
     }
@@ -778,10 +797,10 @@ cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geom
     e = cudaMemsetAsync(scratch, 0, (1 + tiles) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     unsigned grid = tiles == 0 ? 1u : (unsigned)tiles;
-    k_raygen_path<<<grid, kBlock, 0, s>>>(
+    k_raygen_path<-1><<<grid, kBlock, 0, s>>>(
         seeds, geoms, reinterpret_cast<const float4*>(in_rays), reinterpret_cast<float4*>(out_rays), in_i2p,
         out_i2p, reinterpret_cast<const int4*>(in_res), reinterpret_cast<float4*>(decreases), out_count, n,
-        n_dev, albedo, scratch);
+        n_dev, albedo, scratch, nullptr, nullptr, Box6{});
     count_launch();
     return cudaGetLastError();
 }

@@ -19,6 +19,22 @@ struct FrameParams {
     int pad[3];
 };
 
+// Scene box of the Morton keys (min corner and extent per axis).
+struct Box6 {
+    float smin[3];
+    float ssize[3];
+};
+
+// Morton keys written by the path-ray generation for the rays it creates
+// (kind WFPT_MORTON_*; keys[i] and indices[i] = i per output ray i, as
+// launch_morton writes them over the output rays).
+struct MortonOut {
+    int kind;
+    void* keys;
+    uint32_t* indices;
+    Box6 box;
+};
+
 // Number of kernels this library has launched (all threads, all devices).
 void count_launch(uint32_t k = 1);
 uint64_t launch_count();
@@ -42,11 +58,13 @@ cudaError_t launch_raygen_shadow(const uint32_t* seeds, const wfpt_ray* in_rays,
                                  float radius, int bb, int bs, const uint32_t* n_in_dev, int S,
                                  cudaStream_t s);
 size_t raygen_path_scratch_bytes(uint32_t max_n);
+// mo (nullable): also the Morton keys of the output rays (what
+// launch_morton over out_rays and *out_count would write).
 cudaError_t launch_raygen_path(uint32_t* seeds, const wfpt_geometry* geoms, const wfpt_ray* in_rays,
                                wfpt_ray* out_rays, const int32_t* in_i2p, int32_t* out_i2p,
                                const wfpt_hit* in_res, float* decreases, uint32_t* out_count,
                                uint32_t n, const uint32_t* n_dev, float albedo, void* scratch,
-                               cudaStream_t s);
+                               cudaStream_t s, const MortonOut* mo = nullptr);
 // launch_raygen_path over the library's static scratch (n at most
 // WFPT_RAYGEN_PATH_STATIC_MAX_RAYS); calls on one device must not overlap.
 cudaError_t launch_raygen_path_static(uint32_t* seeds, const wfpt_geometry* geoms, const wfpt_ray* in_rays,
