@@ -1143,6 +1143,7 @@ struct Best64 {
 
 static void f64_tri(const double* o, const double* d, int kx, int ky, int kz, double Sx, double Sy, double Sz,
                     const double* tv, uint32_t tri, double tmin, Best64& h, bool& hit) {
+    (void)d;  // the direction enters through the permutation (kx, ky, kz) and the shear (Sx, Sy, Sz)
     double A[3], B[3], C[3];
     for (int k = 0; k < 3; ++k) {
         A[k] = tv[k] - o[k];
